@@ -1,0 +1,278 @@
+"""emc_gb300 -- GB300-native (sm_103a) EMC iteration behind the reference's
+`cuda_*` interface.
+
+Python mirror of the C ABI in include/emc_gb300.h.  `Context` exposes the
+reference's per-function entry points under their reference names
+(emc_cuda_help.h:9-117): get_slices, update_scaling_full,
+calculate_responsabilities, max_vector, respons_max_expf,
+norm_respons_sumexpf, update_slices, divide_model_by_weight,
+normalize_model, model_max, model_average, blur_model, reset_real.  Buffers are
+torch CUDA tensors (device memory and streams only -- every computation is a
+kernel of libemc_gb300.so).  `Plan` drives the fused iteration.
+
+Errors: every call checks the int status and raises EmcError with the
+context's last error text, where the reference printed and continued.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from ._lib import (DIFF_ABSOLUTE, DIFF_POISSON, DIFF_RELATIVE, DIFF_TRUE_POISSON,  # noqa: F401
+                   INSERT_ATOMIC, INSERT_DETERMINISTIC, INTERP_NEAREST, INTERP_TRILINEAR,
+                   PREC_FP32, PREC_MIXED, EmcError, IterStats, PlanDesc)
+
+__all__ = [
+    "Context", "Plan", "EmcError", "generate_rotations", "rotation_count",
+    "calculate_coordinates", "sigma_schedule", "library",
+]
+
+
+def library():
+    return _lib.load()
+
+
+def _ptr(t, dtype=None, name="buffer"):
+    """Raw device pointer of a contiguous CUDA tensor (None -> NULL)."""
+    if t is None:
+        return None
+    if isinstance(t, int):
+        return t
+    if not t.is_cuda:
+        raise EmcError(f"{name} must be a CUDA tensor")
+    if not t.is_contiguous():
+        raise EmcError(f"{name} must be contiguous")
+    if dtype is not None and t.dtype != dtype:
+        raise EmcError(f"{name} must be {dtype}, got {t.dtype}")
+    return t.data_ptr()
+
+
+def rotation_count(n: int) -> int:
+    return int(_lib.load().emc_rotation_count(n))
+
+
+def generate_rotations(n: int):
+    """600-cell sampling at level n (rotations.c:77-458): (quats [R,4], weights [R])."""
+    lib = _lib.load()
+    R = lib.emc_rotation_count(n)
+    if R <= 0:
+        raise EmcError(f"bad rotation level {n}")
+    q = np.zeros((R, 4), np.float32)
+    w = np.zeros(R, np.float32)
+    rc = lib.emc_generate_rotations(n, q.ctypes.data, w.ctypes.data, R)
+    if rc != R:
+        raise EmcError(f"emc_generate_rotations({n}) returned {rc}")
+    return q, w
+
+
+def calculate_coordinates(side: int, pixel_size: float, detector_distance: float,
+                          wavelength: float):
+    """Detector pixel coordinates (emc_helper.cpp:55-79): x, y, z as [side*side] float32."""
+    lib = _lib.load()
+    x = np.zeros(side * side, np.float32)
+    y = np.zeros_like(x)
+    z = np.zeros_like(x)
+    rc = lib.emc_calculate_coordinates(side, pixel_size, detector_distance, wavelength,
+                                       x.ctypes.data, y.ctypes.data, z.ctypes.data)
+    if rc != 0:
+        raise EmcError(f"emc_calculate_coordinates failed ({rc})")
+    return x, y, z
+
+
+def sigma_schedule(iteration: int, sigma_start: float, sigma_final: float, half_life: int) -> float:
+    return float(_lib.load().emc_sigma_schedule(iteration, sigma_start, sigma_final, half_life))
+
+
+class Context:
+    """One device, one stream (replaces cuda_set_device, emc_cuda.cu:867-870)."""
+
+    def __init__(self, device: int = 0):
+        self._lib = _lib.load()
+        h = C.c_void_p()
+        rc = self._lib.emc_ctx_create(C.byref(h), device)
+        if rc != 0:
+            raise EmcError(f"emc_ctx_create(device={device}) failed: {_lib.ERRORS.get(rc, rc)}")
+        self._h = h
+        self.device = device
+
+    # -- plumbing ------------------------------------------------------------
+    @property
+    def handle(self):
+        return self._h
+
+    def _check(self, rc, what):
+        if rc != 0:
+            msg = self._lib.emc_last_error(self._h).decode()
+            raise EmcError(f"{what}: {_lib.ERRORS.get(rc, rc)}: {msg}")
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.emc_ctx_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_stream(self, stream=None):
+        self._check(self._lib.emc_set_stream(self._h, stream), "set_stream")
+
+    @property
+    def stream(self) -> int:
+        return self._lib.emc_get_stream(self._h) or 0
+
+    def sync(self):
+        self._check(self._lib.emc_sync(self._h), "sync")
+
+    @property
+    def kernel_launches(self) -> int:
+        return int(self._lib.emc_kernel_launches(self._h))
+
+    # -- reference entry points ---------------------------------------------
+    def get_slices(self, model, side, slices, rot, x, y, z, start, chunk, interp=INTERP_NEAREST):
+        import torch
+        self._check(self._lib.emc_get_slices(
+            self._h, _ptr(model, torch.float32, "model"), side, _ptr(slices, torch.float32, "slices"),
+            _ptr(rot, torch.float32, "rot"), _ptr(x), _ptr(y), _ptr(z), start, chunk, interp),
+            "get_slices")
+
+    def update_scaling_full(self, images, slices, mask, scaling, n_2d, n_images, start, chunk,
+                            diff=DIFF_POISSON):
+        import torch
+        self._check(self._lib.emc_update_scaling_full(
+            self._h, _ptr(images, torch.float32), _ptr(slices, torch.float32),
+            _ptr(mask, torch.int32, "mask"), _ptr(scaling, torch.float32), n_2d, n_images, start,
+            chunk, diff), "update_scaling_full")
+
+    def calculate_responsabilities(self, slices, images, mask, sigma, scaling, respons, weights,
+                                   n_2d, n_images, start, chunk, diff=DIFF_POISSON):
+        import torch
+        self._check(self._lib.emc_calculate_responsabilities(
+            self._h, _ptr(slices, torch.float32), _ptr(images, torch.float32),
+            _ptr(mask, torch.int32), float(sigma), _ptr(scaling, torch.float32),
+            _ptr(respons, torch.float32), _ptr(weights, torch.float32), n_2d, n_images, start,
+            chunk, diff), "calculate_responsabilities")
+
+    def max_vector(self, respons, n_images, n_slices, maxr):
+        self._check(self._lib.emc_max_vector(self._h, _ptr(respons), n_images, n_slices,
+                                             _ptr(maxr)), "max_vector")
+
+    def respons_max_expf(self, respons, maxv, n_images, n_slices, out_sum):
+        self._check(self._lib.emc_respons_max_expf(self._h, _ptr(respons), _ptr(maxv), n_images,
+                                                   n_slices, _ptr(out_sum)), "respons_max_expf")
+
+    def norm_respons_sumexpf(self, respons, lse, maxv, n_images, n_slices):
+        self._check(self._lib.emc_norm_respons_sumexpf(self._h, _ptr(respons), _ptr(lse),
+                                                       _ptr(maxv), n_images, n_slices),
+                    "norm_respons_sumexpf")
+
+    def log_sum_max(self, out_sum, maxv, lse, n_images):
+        self._check(self._lib.emc_log_sum_max(self._h, _ptr(out_sum), _ptr(maxv), _ptr(lse),
+                                              n_images), "log_sum_max")
+
+    def update_slices(self, images, slices, mask, respons, scaling, active, n_images, start,
+                      chunk, n_2d, side, model, x, y, z, rot_chunk, weight):
+        import torch
+        self._check(self._lib.emc_update_slices(
+            self._h, _ptr(images), _ptr(slices), _ptr(mask, torch.int32), _ptr(respons),
+            _ptr(scaling), _ptr(active, torch.int32, "active"), n_images, start, chunk, n_2d, side,
+            _ptr(model), _ptr(x), _ptr(y), _ptr(z), _ptr(rot_chunk), _ptr(weight)),
+            "update_slices")
+
+    def divide_model_by_weight(self, side, model, weight):
+        self._check(self._lib.emc_divide_model_by_weight(self._h, side, _ptr(model), _ptr(weight)),
+                    "divide_model_by_weight")
+
+    def normalize_model(self, side, model) -> float:
+        m = C.c_float()
+        self._check(self._lib.emc_normalize_model(self._h, side, _ptr(model), C.byref(m)),
+                    "normalize_model")
+        return float(m.value)
+
+    def model_max(self, model, n=None) -> float:
+        m = C.c_float()
+        self._check(self._lib.emc_model_max(self._h, _ptr(model), n or model.numel(), C.byref(m)),
+                    "model_max")
+        return float(m.value)
+
+    def model_average(self, model, n=None) -> float:
+        m = C.c_float()
+        self._check(self._lib.emc_model_average(self._h, _ptr(model), n or model.numel(),
+                                                C.byref(m)), "model_average")
+        return float(m.value)
+
+    def blur_model(self, model, side, sigma):
+        self._check(self._lib.emc_blur_model(self._h, _ptr(model), side, float(sigma)),
+                    "blur_model")
+
+    def reset_real(self, x, n=None):
+        self._check(self._lib.emc_reset_real(self._h, _ptr(x), n if n is not None else x.numel()),
+                    "reset_real")
+
+    def copy_real_d2d(self, dst, src_ptr: int, start: int = 0, n=None):
+        """dst[start:start+n] = n floats at device address src_ptr."""
+        n = dst.numel() - start if n is None else n
+        self._check(self._lib.emc_copy_real_d2d(self._h, _ptr(dst), src_ptr, start, n),
+                    "copy_real_d2d")
+
+    def copy_real_to_host(self, src_ptr: int, n: int) -> np.ndarray:
+        out = np.empty(n, np.float32)
+        self._check(self._lib.emc_copy_real_to_host(self._h, out.ctypes.data, src_ptr, n),
+                    "copy_real_to_host")
+        return out
+
+
+class Plan:
+    """Fused EMC iteration (emc_plan_* in the C ABI)."""
+
+    def __init__(self, ctx: Context, side, n_images, n_rot, diff=DIFF_POISSON,
+                 interp=INTERP_NEAREST, precision=PREC_FP32, insert_mode=INSERT_ATOMIC,
+                 known_intensity=0, normalize_images=0, blur_sigma=0.0):
+        self.ctx = ctx
+        self._lib = ctx._lib
+        d = PlanDesc(side, n_images, n_rot, diff, interp, precision, insert_mode,
+                     known_intensity, normalize_images, float(blur_sigma))
+        self.desc = d
+        h = C.c_void_p()
+        ctx._check(self._lib.emc_plan_create(ctx.handle, C.byref(d), C.byref(h)), "plan_create")
+        self._h = h
+        self._bound = None
+
+    @property
+    def workspace_bytes(self) -> int:
+        return int(self._lib.emc_plan_workspace_bytes(self._h))
+
+    def bind(self, images, mask, x, y, z, rot, rot_weights):
+        import torch
+        self._bound = (images, mask, x, y, z, rot, rot_weights)  # keep alive
+        self.ctx._check(self._lib.emc_plan_bind(
+            self._h, _ptr(images, torch.float32, "images"), _ptr(mask, torch.int32, "mask"),
+            _ptr(x), _ptr(y), _ptr(z), _ptr(rot, torch.float32, "rot"),
+            _ptr(rot_weights, torch.float32, "rot_weights")), "plan_bind")
+
+    def iterate(self, model, weight, sigma, stats: bool = True):
+        st = IterStats()
+        self.ctx._check(self._lib.emc_iterate(self._h, _ptr(model), _ptr(weight), float(sigma),
+                                              C.byref(st) if stats else None), "iterate")
+        return st if stats else None
+
+    def results(self):
+        r, s, l = C.c_void_p(), C.c_void_p(), C.c_void_p()
+        self.ctx._check(self._lib.emc_plan_results(self._h, C.byref(r), C.byref(s), C.byref(l)),
+                        "plan_results")
+        return r.value, s.value, l.value
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.emc_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

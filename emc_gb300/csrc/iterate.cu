@@ -1,0 +1,1099 @@
+// The fused EMC iteration (emc_plan_* / emc_iterate) and its FP32 kernels.
+//
+// One iteration restates main.cpp:239-480 for one process on one GPU:
+//   expand        slice the model at every rotation, compacted to the
+//                 P_eff pixels with mask != 0                       (A4)
+//   scaling +     one tiled kernel per 128x128 (rotation, pattern) tile:
+//   likelihood    pass 1 accumulates phi = sum k^2 / sum k s, pass 2 the
+//                 per-pixel difference sum, the epilogue writes L and phi
+//                 and a per-tile (max, sum exp) pair for every pattern (A5, A6)
+//   normalise     FP64 log-sum-exp over the tile partials -> lse_i,
+//                 P = exp(L - lse), Q = P / phi, T_r = sum_i P      (A7-A9)
+//   M-step        tiled GEMM U = Q K over the compacted pixels; its epilogue
+//                 inserts T_r * (U / T_r) into the model and T_r into the
+//                 weight (nearest or trilinear; float or fixed-point
+//                 atomics)                                           (A10, A11)
+//   finish        divide by weight, normalise to mean 1 (FP64), blur (A13-A15)
+// The MPI exchanges of the reference (main.cpp:367-392, 467-480) have no
+// counterpart: the normaliser and the model sums are device reductions.
+//
+// Semantics of the fused path (the "intended" forms, stated because they
+// differ from the drop-in kernels): the scaling denominator is a float sum
+// (the reference truncates it to int), the per-pixel term is FP32, pairs with
+// no overlap (count_r == 0) or undefined scaling (num or den <= 0) get
+// L = -inf and phi = 1, a pattern whose pairs are all invalid gets zero
+// responsibility, and the normaliser is FP64.
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "geometry.cuh"
+#include "kernels.cuh"
+#include "plan.cuh"
+
+namespace emc {
+
+int plan_alloc(emc_plan* p, void** ptr, size_t bytes) {
+  if (bytes == 0) bytes = 256;
+  cudaError_t e = cudaMalloc(ptr, bytes);
+  if (e != cudaSuccess)
+    return fail(p->ctx, EMC_ERR_NOMEM, "plan alloc of %zu bytes: %s", bytes, cudaGetErrorString(e));
+  p->allocs.push_back(*ptr);
+  p->bytes += bytes;
+  return EMC_OK;
+}
+
+template <typename T>
+static int alloc_n(emc_plan* p, T** ptr, size_t n) {
+  return plan_alloc(p, (void**)ptr, n * sizeof(T));
+}
+
+// ------------------------------------------------------------- bind ------
+__global__ void gather_coords_kernel(const int* __restrict__ pix, const float* __restrict__ x,
+                                     const float* __restrict__ y, const float* __restrict__ z,
+                                     float* cx, float* cy, float* cz, int Kp) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= Kp) return;
+  const int p = pix[q];
+  cx[q] = p >= 0 ? x[p] : 0.0f;
+  cy[q] = p >= 0 ? y[p] : 0.0f;
+  cz[q] = p >= 0 ? z[p] : 0.0f;
+}
+
+// Per-pattern factor of the reference's image normalisation
+// (emc_helper.cpp:389-418): c_i = N_2d / (float sum over mask == 1 pixels).
+__global__ void pattern_norm_kernel(const float* __restrict__ images, const int* __restrict__ mask,
+                                    int n2, int N, int normalize, float* __restrict__ cnorm) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  float c = 1.0f;
+  if (normalize) {
+    const float* img = images + (size_t)i * n2;
+    float s = 0.0f;
+    for (int p = 0; p < n2; ++p)
+      if (__ldg(mask + p) == 1) s = __fadd_rn(s, __ldg(img + p));
+    c = __fdiv_rn((float)n2, s);
+  }
+  cnorm[i] = c;
+}
+
+// Compacted pattern operands.  flags[0] bit 0: non-finite input; bit 1: a
+// count outside [0, 2048] or not an integer (no exact FP16 form).
+__global__ void pattern_ops_kernel(const float* __restrict__ images, const int* __restrict__ pix,
+                                   const float* __restrict__ cnorm, int n2, int N, int Kp,
+                                   float* __restrict__ Kraw, float* __restrict__ Kt,
+                                   float* __restrict__ K2, int* __restrict__ flags) {
+  const int i = blockIdx.y;
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= Kp) return;
+  const int p = pix[q];
+  float k = 0.0f;
+  if (p >= 0) {
+    const float v = __ldg(images + (size_t)i * n2 + p);
+    if (!isfinite(v)) atomicOr(flags, 1);
+    if (!(v >= 0.0f && v <= 2048.0f && v == rintf(v))) atomicOr(flags, 2);
+    k = __fmul_rn(v, __ldg(cnorm + i));
+  }
+  const size_t o = (size_t)i * Kp + q;
+  Kraw[o] = k;
+  const float kt = (double)k > 1e-10 ? k : 0.0f;
+  if (Kt) Kt[o] = kt;
+  if (K2) K2[o] = __fmul_rn(kt, kt);
+}
+
+__global__ void row_sum_kernel(const float* __restrict__ a, int ncol, int ld,
+                               float* __restrict__ out) {
+  const int r = blockIdx.x;
+  double s = 0.0;
+  for (int c = threadIdx.x; c < ncol; c += blockDim.x) s += (double)a[(size_t)r * ld + c];
+  __shared__ double sh[256];
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[r] = (float)sh[0];
+}
+
+// ------------------------------------------------------------ expand -----
+constexpr float kPoisC = 0.02f;       // emc_cuda.cu:205
+constexpr float kSliceFloor = 1e-6f;  // true-Poisson floor for unknown voxels
+
+template <int INTERP>
+__device__ __forceinline__ float plan_sample(const float* __restrict__ model, int side,
+                                             const RotMat& R, float x, float y, float z);
+
+template <>
+__device__ __forceinline__ float plan_sample<EMC_INTERP_NEAREST>(const float* __restrict__ model,
+                                                                  int side, const RotMat& R,
+                                                                  float x, float y, float z) {
+  const long ix = lroundf(voxel_coord(side, rotate_row(R, 0, x, y, z)));
+  const long iy = lroundf(voxel_coord(side, rotate_row(R, 1, x, y, z)));
+  const long iz = lroundf(voxel_coord(side, rotate_row(R, 2, x, y, z)));
+  if (ix > 0 && ix < side && iy > 0 && iy < side && iz > 0 && iz < side)
+    return __ldg(model + ((size_t)iz * side + iy) * side + ix);
+  return -1.0f;
+}
+
+template <>
+__device__ __forceinline__ float plan_sample<EMC_INTERP_TRILINEAR>(const float* __restrict__ model,
+                                                                    int side, const RotMat& R,
+                                                                    float x, float y, float z) {
+  const float cx = voxel_coord(side, rotate_row(R, 0, x, y, z));
+  const float cy = voxel_coord(side, rotate_row(R, 1, x, y, z));
+  const float cz = voxel_coord(side, rotate_row(R, 2, x, y, z));
+  const float fx0 = floorf(cx), fy0 = floorf(cy), fz0 = floorf(cz);
+  const int x0 = (int)fx0, y0 = (int)fy0, z0 = (int)fz0;
+  const float tx = cx - fx0, ty = cy - fy0, tz = cz - fz0;
+  float acc = 0.0f, wsum = 0.0f;
+#pragma unroll
+  for (int c = 0; c < 8; ++c) {
+    const int xi = x0 + (c & 1), yi = y0 + ((c >> 1) & 1), zi = z0 + (c >> 2);
+    if (xi < 0 || xi >= side || yi < 0 || yi >= side || zi < 0 || zi >= side) continue;
+    const float w = ((c & 1) ? tx : 1.0f - tx) * (((c >> 1) & 1) ? ty : 1.0f - ty) *
+                    ((c >> 2) ? tz : 1.0f - tz);
+    const float v = __ldg(model + ((size_t)zi * side + yi) * side + xi);
+    if (v < 0.0f || w <= 0.0f) continue;
+    acc = __fmaf_rn(w, v, acc);
+    wsum += w;
+  }
+  return wsum > 1e-6f ? acc / wsum : -1.0f;
+}
+
+// One block per rotation: the compacted slice row S[r][0..Kp) and the
+// per-rotation sums: count_r (s > 0), A_r = sum s^2/(s+c) and the floored
+// slice sum of the true-Poisson likelihood.
+template <int INTERP>
+__global__ void __launch_bounds__(256) slice_rows_kernel(
+    const float* __restrict__ model, int side, const float* __restrict__ rot,
+    const int* __restrict__ pix, const float* __restrict__ cx, const float* __restrict__ cy,
+    const float* __restrict__ cz, int R, int Kp, float* __restrict__ S,
+    float* __restrict__ rot_cnt, float* __restrict__ rot_A, float* __restrict__ rot_ssum) {
+  const int r = blockIdx.x;
+  __shared__ RotMat sR;
+  if (threadIdx.x == 0) sR = quat_to_matrix(rot + 4 * (size_t)r);
+  __syncthreads();
+  const RotMat Rm = sR;
+  double cnt = 0.0, A = 0.0, ss = 0.0;
+  for (int q = threadIdx.x; q < Kp; q += blockDim.x) {
+    float s = 0.0f;
+    if (__ldg(pix + q) >= 0) {
+      s = plan_sample<INTERP>(model, side, Rm, __ldg(cx + q), __ldg(cy + q), __ldg(cz + q));
+      if (s > 0.0f) {
+        cnt += 1.0;
+        A += (double)s * s / ((double)s + kPoisC);
+      }
+      ss += (double)fmaxf(s, kSliceFloor);
+    }
+    S[(size_t)r * Kp + q] = s;
+  }
+  __shared__ double sh[3][256];
+  sh[0][threadIdx.x] = cnt;
+  sh[1][threadIdx.x] = A;
+  sh[2][threadIdx.x] = ss;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) {
+      sh[0][threadIdx.x] += sh[0][threadIdx.x + o];
+      sh[1][threadIdx.x] += sh[1][threadIdx.x + o];
+      sh[2][threadIdx.x] += sh[2][threadIdx.x + o];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    rot_cnt[r] = (float)sh[0][0];
+    rot_A[r] = (float)sh[1][0];
+    rot_ssum[r] = (float)sh[2][0];
+  }
+}
+
+// --------------------------------------------------- FP32 E-step tile ----
+constexpr int BM = 128, BN = 128, BK = 16, TPB = 256, SP = BM + 4;
+
+// Loads a [128 rows][16 cols] tile of a row-major matrix (leading dim ld,
+// ld % 4 == 0) into two float4 per thread; rows >= nrows read as zero.
+__device__ __forceinline__ void ld_tile(const float* __restrict__ src, size_t ld, int row0,
+                                        int nrows, int k0, float4 (&v)[2]) {
+#pragma unroll
+  for (int u = 0; u < 2; ++u) {
+    const int f = threadIdx.x + u * TPB;
+    const int row = f >> 2, quad = f & 3;
+    v[u] = row0 + row < nrows
+               ? __ldg(reinterpret_cast<const float4*>(src + (size_t)(row0 + row) * ld + k0) + quad)
+               : make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+}
+
+// Transposed store of a loaded tile: dst[k][row] = op(v).
+template <typename Op>
+__device__ __forceinline__ void st_tile_t(float (*dst)[SP], const float4 (&v)[2], Op op) {
+#pragma unroll
+  for (int u = 0; u < 2; ++u) {
+    const int f = threadIdx.x + u * TPB;
+    const int row = f >> 2, quad = f & 3;
+    dst[quad * 4 + 0][row] = op(v[u].x);
+    dst[quad * 4 + 1][row] = op(v[u].y);
+    dst[quad * 4 + 2][row] = op(v[u].z);
+    dst[quad * 4 + 3][row] = op(v[u].w);
+  }
+}
+
+__device__ __forceinline__ void ld8(const float (*s)[SP], int k, int base, float (&o)[8]) {
+  const float4 a = *reinterpret_cast<const float4*>(&s[k][base]);
+  const float4 b = *reinterpret_cast<const float4*>(&s[k][64 + base]);
+  o[0] = a.x; o[1] = a.y; o[2] = a.z; o[3] = a.w;
+  o[4] = b.x; o[5] = b.y; o[6] = b.z; o[7] = b.w;
+}
+
+__device__ __forceinline__ int micro_idx(int t4, int i) { return (i < 4 ? 0 : 64) + t4 + (i & 3); }
+
+struct EstepArgs {
+  const float* S;      // [Rp][Kp]
+  const float* Kraw;   // [N][Kp]
+  const float* Kt;
+  const float* K2;
+  const float* Ksum;   // [N]
+  const float* rot_cnt;
+  const float* rot_ssum;
+  const float* rotw;   // [R]
+  float* L;            // [R][N]
+  float* PHI;          // [R][N]
+  float2* part;        // [n_rt][N]
+  int* bad;            // invalid pair counter
+  int R, N, Kp;
+  float inv2s2;        // 1 / (2 sigma^2)
+  int known_intensity;
+};
+
+// Writes L/phi of the micro-tile and the tile's (max, sum exp) per pattern.
+__device__ void estep_epilogue(const EstepArgs& a, float (&Lv)[8][8], float (&phi)[8][8],
+                               float* sred /* [16][128] */, float* scol /* [128] */) {
+  const int ty = threadIdx.x >> 4, tx = threadIdx.x & 15;
+  const int r0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+  const int ty4 = ty * 4, tx4 = tx * 4;
+  // stores
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const int r = r0 + micro_idx(ty4, i);
+    if (r >= a.R) continue;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int n = n0 + h * 64 + tx4;
+      float* lp = a.L + (size_t)r * a.N + n;
+      float* pp = a.PHI + (size_t)r * a.N + n;
+      if (n + 3 < a.N && ((a.N & 3) == 0)) {
+        *reinterpret_cast<float4*>(lp) =
+            make_float4(Lv[i][4 * h], Lv[i][4 * h + 1], Lv[i][4 * h + 2], Lv[i][4 * h + 3]);
+        *reinterpret_cast<float4*>(pp) =
+            make_float4(phi[i][4 * h], phi[i][4 * h + 1], phi[i][4 * h + 2], phi[i][4 * h + 3]);
+      } else {
+        for (int c = 0; c < 4; ++c)
+          if (n + c < a.N) {
+            lp[c] = Lv[i][4 * h + c];
+            pp[c] = phi[i][4 * h + c];
+          }
+      }
+    }
+  }
+  // per-pattern max over the tile's rotations
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    float m = -INFINITY;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) m = fmaxf(m, Lv[i][j]);
+    sred[ty * BN + micro_idx(tx4, j)] = m;
+  }
+  __syncthreads();
+  if (threadIdx.x < BN) {
+    float m = -INFINITY;
+    for (int t = 0; t < 16; ++t) m = fmaxf(m, sred[t * BN + threadIdx.x]);
+    scol[threadIdx.x] = m;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    const float m = scol[micro_idx(tx4, j)];
+    float s = 0.0f;
+    if (m > -INFINITY) {
+#pragma unroll
+      for (int i = 0; i < 8; ++i) s += expf(Lv[i][j] - m);
+    }
+    sred[ty * BN + micro_idx(tx4, j)] = s;
+  }
+  __syncthreads();
+  if (threadIdx.x < BN) {
+    const int n = n0 + threadIdx.x;
+    float s = 0.0f;
+    for (int t = 0; t < 16; ++t) s += sred[t * BN + threadIdx.x];
+    if (n < a.N) a.part[(size_t)blockIdx.y * a.N + n] = make_float2(scol[threadIdx.x], s);
+  }
+}
+
+// Reference-"poisson" likelihood with per-pair scaling, two pixel passes.
+__global__ void __launch_bounds__(TPB, 1) estep_fp32_kernel(EstepArgs a) {
+  __shared__ __align__(16) float s0[BK][SP];
+  __shared__ __align__(16) float s1[BK][SP];
+  __shared__ __align__(16) float s2[BK][SP];
+  __shared__ __align__(16) float s3[BK][SP];
+  const int ty = threadIdx.x >> 4, tx = threadIdx.x & 15;
+  const int ty4 = ty * 4, tx4 = tx * 4;
+  const int r0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+
+  float num[8][8], den[8][8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+#pragma unroll
+    for (int j = 0; j < 8; ++j) num[i][j] = den[i][j] = 0.0f;
+
+  float4 vr[2], vk2[2], vkt[2];
+  const int nk = a.Kp / BK;
+  if (!a.known_intensity) {
+    // ---- pass 1: num = sum Kt^2 [s > 1e-10], den = sum Kt s [s > 1e-10]
+    ld_tile(a.S, a.Kp, r0, a.R, 0, vr);
+    ld_tile(a.K2, a.Kp, n0, a.N, 0, vk2);
+    ld_tile(a.Kt, a.Kp, n0, a.N, 0, vkt);
+    for (int kb = 0; kb < nk; ++kb) {
+      st_tile_t(s0, vr, [](float s) { return (double)s > 1e-10 ? 1.0f : 0.0f; });
+      st_tile_t(s1, vr, [](float s) { return (double)s > 1e-10 ? s : 0.0f; });
+      st_tile_t(s2, vk2, [](float v) { return v; });
+      st_tile_t(s3, vkt, [](float v) { return v; });
+      __syncthreads();
+      if (kb + 1 < nk) {
+        ld_tile(a.S, a.Kp, r0, a.R, (kb + 1) * BK, vr);
+        ld_tile(a.K2, a.Kp, n0, a.N, (kb + 1) * BK, vk2);
+        ld_tile(a.Kt, a.Kp, n0, a.N, (kb + 1) * BK, vkt);
+      }
+#pragma unroll 4
+      for (int k = 0; k < BK; ++k) {
+        float ra[8], rb[8], pk2[8], pkt[8];
+        ld8(s0, k, ty4, ra);
+        ld8(s1, k, ty4, rb);
+        ld8(s2, k, tx4, pk2);
+        ld8(s3, k, tx4, pkt);
+#pragma unroll
+        for (int i = 0; i < 8; ++i)
+#pragma unroll
+          for (int j = 0; j < 8; ++j) {
+            num[i][j] = __fmaf_rn(pk2[j], ra[i], num[i][j]);
+            den[i][j] = __fmaf_rn(pkt[j], rb[i], den[i][j]);
+          }
+      }
+      __syncthreads();
+    }
+  }
+  // 1/phi into num, phi into den (phi = 1 when known or undefined)
+  int nbad = 0;
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      float phi = 1.0f, iphi = 1.0f;
+      if (!a.known_intensity) {
+        const bool ok = num[i][j] > 0.0f && den[i][j] > 0.0f;
+        phi = ok ? __fdiv_rn(num[i][j], den[i][j]) : 1.0f;
+        iphi = ok ? __fdiv_rn(den[i][j], num[i][j]) : -1.0f;  // -1 marks invalid
+      }
+      num[i][j] = iphi;
+      den[i][j] = phi;
+    }
+  // ---- pass 2: acc = sum (s - k/phi)^2 / (s + c) over s > 0
+  float acc[8][8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+#pragma unroll
+    for (int j = 0; j < 8; ++j) acc[i][j] = 0.0f;
+  ld_tile(a.S, a.Kp, r0, a.R, 0, vr);
+  ld_tile(a.Kraw, a.Kp, n0, a.N, 0, vk2);
+  for (int kb = 0; kb < nk; ++kb) {
+    st_tile_t(s0, vr, [](float s) { return s; });
+    st_tile_t(s1, vr, [](float s) { return s > 0.0f ? __frcp_rn(s + kPoisC) : 0.0f; });
+    st_tile_t(s2, vk2, [](float v) { return v; });
+    __syncthreads();
+    if (kb + 1 < nk) {
+      ld_tile(a.S, a.Kp, r0, a.R, (kb + 1) * BK, vr);
+      ld_tile(a.Kraw, a.Kp, n0, a.N, (kb + 1) * BK, vk2);
+    }
+#pragma unroll 4
+    for (int k = 0; k < BK; ++k) {
+      float rs[8], rg[8], pk[8];
+      ld8(s0, k, ty4, rs);
+      ld8(s1, k, ty4, rg);
+      ld8(s2, k, tx4, pk);
+#pragma unroll
+      for (int i = 0; i < 8; ++i)
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          const float d = __fmaf_rn(-pk[j], num[i][j], rs[i]);
+          const float t = __fmul_rn(d, rg[i]);
+          acc[i][j] = __fmaf_rn(t, d, acc[i][j]);
+        }
+    }
+    __syncthreads();
+  }
+  // ---- epilogue
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const int r = r0 + micro_idx(ty4, i);
+    const bool rok = r < a.R;
+    const float cnt = rok ? __ldg(a.rot_cnt + r) : 0.0f;
+    const float lw = rok ? logf(__ldg(a.rotw + r)) : 0.0f;
+    const float scale = cnt > 0.0f ? a.inv2s2 / cnt : 0.0f;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const int n = n0 + micro_idx(tx4, j);
+      const bool ok = rok && n < a.N && cnt > 0.0f && num[i][j] > 0.0f;
+      if (rok && n < a.N && !ok) nbad++;
+      acc[i][j] = ok ? lw - acc[i][j] * scale : -INFINITY;
+    }
+  }
+  if (nbad) atomicAdd(a.bad, nbad);
+  float* sred = &s0[0][0];  // 16 x 128 floats fit in s0..s3 (4 x 16 x 132)
+  float* scol = &s3[0][0];
+  estep_epilogue(a, acc, den, sred, scol);
+}
+
+// True-Poisson likelihood: L = log w + sum k log s + K log(K/S_r) - K.
+__global__ void __launch_bounds__(TPB, 1) estep_pois_fp32_kernel(EstepArgs a) {
+  __shared__ __align__(16) float s0[BK][SP];
+  __shared__ __align__(16) float s2[BK][SP];
+  __shared__ __align__(16) float s4[BK][SP];
+  const int ty = threadIdx.x >> 4, tx = threadIdx.x & 15;
+  const int ty4 = ty * 4, tx4 = tx * 4;
+  const int r0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+  float acc[8][8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+#pragma unroll
+    for (int j = 0; j < 8; ++j) acc[i][j] = 0.0f;
+  float4 vr[2], vk[2];
+  const int nk = a.Kp / BK;
+  ld_tile(a.S, a.Kp, r0, a.R, 0, vr);
+  ld_tile(a.Kraw, a.Kp, n0, a.N, 0, vk);
+  for (int kb = 0; kb < nk; ++kb) {
+    st_tile_t(s0, vr, [](float s) { return __logf(fmaxf(s, kSliceFloor)); });
+    st_tile_t(s2, vk, [](float v) { return v; });
+    __syncthreads();
+    if (kb + 1 < nk) {
+      ld_tile(a.S, a.Kp, r0, a.R, (kb + 1) * BK, vr);
+      ld_tile(a.Kraw, a.Kp, n0, a.N, (kb + 1) * BK, vk);
+    }
+#pragma unroll 4
+    for (int k = 0; k < BK; ++k) {
+      float rl[8], pk[8];
+      ld8(s0, k, ty4, rl);
+      ld8(s2, k, tx4, pk);
+#pragma unroll
+      for (int i = 0; i < 8; ++i)
+#pragma unroll
+        for (int j = 0; j < 8; ++j) acc[i][j] = __fmaf_rn(pk[j], rl[i], acc[i][j]);
+    }
+    __syncthreads();
+  }
+  float phi[8][8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const int r = r0 + micro_idx(ty4, i);
+    const bool rok = r < a.R;
+    const float lw = rok ? logf(__ldg(a.rotw + r)) : 0.0f;
+    const float Sr = rok ? __ldg(a.rot_ssum + r) : 1.0f;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const int n = n0 + micro_idx(tx4, j);
+      const float Ki = n < a.N ? __ldg(a.Ksum + n) : 0.0f;
+      float l, f;
+      if (a.known_intensity) {
+        f = 1.0f;
+        l = lw + acc[i][j] - Sr;
+      } else if (Ki > 0.0f) {
+        f = Ki / Sr;
+        l = lw + acc[i][j] + Ki * logf(f) - Ki;
+      } else {
+        f = 0.0f;
+        l = lw;
+      }
+      acc[i][j] = rok && n < a.N ? l : -INFINITY;
+      phi[i][j] = f;
+    }
+  }
+  float* sred = &s0[0][0];
+  float* scol = &s4[0][0];
+  estep_epilogue(a, acc, phi, sred, scol);
+}
+
+// ------------------------------------------------------- normalise -------
+// lse_i = M + log(sum_t s_t exp(m_t - M)) over the rotation tiles, FP64.
+// Patterns with no valid pair get lse = +inf (all responsibilities 0).
+__global__ void lse_combine_kernel(const float2* __restrict__ part, int n_rt, int N,
+                                   double* __restrict__ lse) {
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= N) return;
+  float M = -INFINITY;
+  for (int t = 0; t < n_rt; ++t) M = fmaxf(M, part[(size_t)t * N + n].x);
+  double l = INFINITY;
+  if (M > -INFINITY) {
+    double s = 0.0;
+    for (int t = 0; t < n_rt; ++t) {
+      const float2 v = part[(size_t)t * N + n];
+      if (v.x > -INFINITY) s += (double)v.y * exp((double)v.x - (double)M);
+    }
+    l = (double)M + log(s);
+  }
+  lse[n] = l;
+}
+
+// Deterministic FP64 sum of the finite entries of x[0..n) into out[0]
+// (one block; the order of additions is fixed).
+__global__ void finite_sum_kernel(const double* __restrict__ x, int n, double* __restrict__ out) {
+  __shared__ double sh[256];
+  double s = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x)
+    if (isfinite(x[i])) s += x[i];
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[0] = sh[0];
+}
+
+// One block per rotation row: P = exp(L - lse) (in place), Q = P / phi
+// (row stride ldq, zero padded), T_r = sum_i P, and the row's captured mass
+// and inserted-mass bound sum_i Q_ri K_i (FP64).
+__global__ void __launch_bounds__(256) mprep_kernel(float* __restrict__ L,
+                                                    const float* __restrict__ PHI,
+                                                    const double* __restrict__ lse,
+                                                    const float* __restrict__ Ksum, int R, int N,
+                                                    float* __restrict__ Q, int ldq,
+                                                    float* __restrict__ T,
+                                                    double* __restrict__ row_mass,
+                                                    double* __restrict__ row_bound) {
+  const int r = blockIdx.x;
+  double t = 0.0, b = 0.0;
+  for (int i = threadIdx.x; i < ldq; i += blockDim.x) {
+    float q = 0.0f;
+    if (i < N) {
+      const size_t e = (size_t)r * N + i;
+      const double li = lse[i];
+      const float l = L[e];
+      float P = 0.0f;
+      if (isfinite(li) && l > -INFINITY) P = (float)exp((double)l - li);
+      L[e] = P;
+      const float f = PHI[e];
+      q = f > 0.0f ? __fdiv_rn(P, f) : 0.0f;
+      t += (double)P;
+      b += (double)q * (double)__ldg(Ksum + i);
+    }
+    if (Q) Q[(size_t)r * ldq + i] = q;
+  }
+  __shared__ double sh[2][256];
+  sh[0][threadIdx.x] = t;
+  sh[1][threadIdx.x] = b;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) {
+      sh[0][threadIdx.x] += sh[0][threadIdx.x + o];
+      sh[1][threadIdx.x] += sh[1][threadIdx.x + o];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    T[r] = (float)sh[0][0];
+    row_mass[r] = sh[0][0];
+    row_bound[r] = sh[1][0];
+  }
+}
+
+// ---------------------------------------------------------- insert -------
+struct InsertCtx {
+  float* model;
+  float* weight;
+  unsigned long long* fix_m;
+  unsigned long long* fix_w;
+  double scale_m, scale_w;  // fixed-point scales (deterministic mode)
+  int side;
+  int interp;
+  int deterministic;
+};
+
+__device__ __forceinline__ void add_voxel(const InsertCtx& c, size_t v, float val, float w) {
+  if (c.deterministic) {
+    atomicAdd(c.fix_m + v, (unsigned long long)__double2ll_rn((double)val * c.scale_m));
+    atomicAdd(c.fix_w + v, (unsigned long long)__double2ll_rn((double)w * c.scale_w));
+  } else {
+    atomicAdd(c.model + v, val);
+    atomicAdd(c.weight + v, w);
+  }
+}
+
+// Inserts value `val` with weight `w` at the detector point (x, y, z) rotated
+// by R: nearest voxel with the reference's insertion bounds (>= 0,
+// emc_atomic.cu:67-69) or a trilinear splat.
+__device__ __forceinline__ void insert_point(const InsertCtx& c, const RotMat& R, float x, float y,
+                                             float z, float val, float w) {
+  const int side = c.side;
+  if (c.interp == EMC_INTERP_NEAREST) {
+    const long ix = lroundf(voxel_coord(side, rotate_row(R, 0, x, y, z)));
+    const long iy = lroundf(voxel_coord(side, rotate_row(R, 1, x, y, z)));
+    const long iz = lroundf(voxel_coord(side, rotate_row(R, 2, x, y, z)));
+    if (ix < 0 || ix >= side || iy < 0 || iy >= side || iz < 0 || iz >= side) return;
+    add_voxel(c, ((size_t)iz * side + iy) * side + ix, val, w);
+  } else {
+    const float cx = voxel_coord(side, rotate_row(R, 0, x, y, z));
+    const float cy = voxel_coord(side, rotate_row(R, 1, x, y, z));
+    const float cz = voxel_coord(side, rotate_row(R, 2, x, y, z));
+    const float fx0 = floorf(cx), fy0 = floorf(cy), fz0 = floorf(cz);
+    const int x0 = (int)fx0, y0 = (int)fy0, z0 = (int)fz0;
+    const float tx = cx - fx0, ty = cy - fy0, tz = cz - fz0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      const int xi = x0 + (k & 1), yi = y0 + ((k >> 1) & 1), zi = z0 + (k >> 2);
+      if (xi < 0 || xi >= side || yi < 0 || yi >= side || zi < 0 || zi >= side) continue;
+      const float f = ((k & 1) ? tx : 1.0f - tx) * (((k >> 1) & 1) ? ty : 1.0f - ty) *
+                      ((k >> 2) ? tz : 1.0f - tz);
+      if (f <= 0.0f) continue;
+      add_voxel(c, ((size_t)zi * side + yi) * side + xi, val * f, w * f);
+    }
+  }
+}
+
+// ---------------------------------------------------- FP32 M-step --------
+struct MstepArgs {
+  const float* Q;     // [R][ldq]
+  const float* Kraw;  // [N][Kp]
+  const float* T;     // [R]
+  const float* rot;   // [4R]
+  const float *cx, *cy, *cz;  // [Kp]
+  int R, N, Kp, ldq, P_eff;
+  InsertCtx ins;
+};
+
+// U = Q K for a 128-rotation x 128-pixel tile, inserted in the epilogue.
+__global__ void __launch_bounds__(TPB, 1) mstep_fp32_kernel(MstepArgs a) {
+  __shared__ __align__(16) float sq[BK][SP];
+  __shared__ __align__(16) float sk[BK][SP];
+  __shared__ RotMat sR[BM];
+  const int ty = threadIdx.x >> 4, tx = threadIdx.x & 15;
+  const int ty4 = ty * 4, tx4 = tx * 4;
+  const int r0 = blockIdx.y * BM, q0 = blockIdx.x * BN;
+  if (threadIdx.x < BM) {
+    const int r = r0 + threadIdx.x;
+    if (r < a.R) sR[threadIdx.x] = quat_to_matrix(a.rot + 4 * (size_t)r);
+  }
+  float acc[8][8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+#pragma unroll
+    for (int j = 0; j < 8; ++j) acc[i][j] = 0.0f;
+  float4 vq[2], vk[2];
+  const int nk = (a.N + BK - 1) / BK;
+  auto ld_k = [&](int kb) {
+    // [16 pattern rows][128 pixels]: 512 float4, thread t: f = t, t + 256
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      const int f = threadIdx.x + u * TPB;
+      const int row = f >> 5, c4 = f & 31;
+      const int i = kb * BK + row;
+      vk[u] = i < a.N ? __ldg(reinterpret_cast<const float4*>(a.Kraw + (size_t)i * a.Kp + q0) + c4)
+                      : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+  };
+  auto st_k = [&]() {
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      const int f = threadIdx.x + u * TPB;
+      const int row = f >> 5, c4 = f & 31;
+      *reinterpret_cast<float4*>(&sk[row][c4 * 4]) = vk[u];
+    }
+  };
+  ld_tile(a.Q, a.ldq, r0, a.R, 0, vq);
+  ld_k(0);
+  for (int kb = 0; kb < nk; ++kb) {
+    st_tile_t(sq, vq, [](float v) { return v; });
+    st_k();
+    __syncthreads();
+    if (kb + 1 < nk) {
+      ld_tile(a.Q, a.ldq, r0, a.R, (kb + 1) * BK, vq);
+      ld_k(kb + 1);
+    }
+#pragma unroll 4
+    for (int k = 0; k < BK; ++k) {
+      float rq[8], pk[8];
+      ld8(sq, k, ty4, rq);
+      ld8(sk, k, tx4, pk);
+#pragma unroll
+      for (int i = 0; i < 8; ++i)
+#pragma unroll
+        for (int j = 0; j < 8; ++j) acc[i][j] = __fmaf_rn(rq[i], pk[j], acc[i][j]);
+    }
+    __syncthreads();
+  }
+  // ---- epilogue: slice = U / T_r, insert T_r * slice with weight T_r
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const int rl = micro_idx(ty4, i);
+    const int r = r0 + rl;
+    if (r >= a.R) continue;
+    const float t = __ldg(a.T + r);
+    if (!(t > 1e-10f)) continue;
+    const RotMat R = sR[rl];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const int q = q0 + micro_idx(tx4, j);
+      if (q >= a.P_eff) continue;
+      const float slice = __fdiv_rn(acc[i][j], t);
+      insert_point(a.ins, R, __ldg(a.cx + q), __ldg(a.cy + q), __ldg(a.cz + q),
+                   __fmul_rn(t, slice), t);
+    }
+  }
+}
+
+// ------------------------------------------------------- finishing -------
+__global__ void fixed_to_model_kernel(const unsigned long long* __restrict__ fm,
+                                      const unsigned long long* __restrict__ fw, double inv_m,
+                                      double inv_w, float* __restrict__ model,
+                                      float* __restrict__ weight, long long n) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += stride) {
+    model[v] = (float)((double)(long long)fm[v] * inv_m);
+    weight[v] = (float)((double)(long long)fw[v] * inv_w);
+  }
+}
+
+}  // namespace emc
+
+using namespace emc;
+
+// ======================================================= C ABI ===========
+extern "C" int emc_plan_create(emc_ctx* ctx, const emc_plan_desc* desc, emc_plan** out) {
+  EMC_CHECK_CTX(ctx);
+  EMC_REQUIRE(ctx, desc && out, "plan_create: null argument");
+  *out = nullptr;
+  const emc_plan_desc& d = *desc;
+  EMC_REQUIRE(ctx, d.side > 1 && d.side <= 1024, "plan_create: side %d out of range", d.side);
+  EMC_REQUIRE(ctx, d.n_images > 0 && d.n_rot > 0, "plan_create: empty problem");
+  EMC_REQUIRE(ctx, d.n_rot <= 65535 * EMC_RT && (long long)d.n_rot * d.n_images < (1LL << 40),
+              "plan_create: problem too large");
+  EMC_REQUIRE(ctx, d.diff == EMC_DIFF_POISSON || d.diff == EMC_DIFF_TRUE_POISSON,
+              "plan_create: diff %d not supported by the fused path", d.diff);
+  EMC_REQUIRE(ctx, d.interp == EMC_INTERP_NEAREST || d.interp == EMC_INTERP_TRILINEAR,
+              "plan_create: bad interp");
+  EMC_REQUIRE(ctx, d.precision == EMC_PREC_FP32 || d.precision == EMC_PREC_MIXED,
+              "plan_create: bad precision");
+  EMC_REQUIRE(ctx, d.insert_mode == EMC_INSERT_ATOMIC || d.insert_mode == EMC_INSERT_DETERMINISTIC,
+              "plan_create: bad insert mode");
+  EMC_REQUIRE(ctx, d.blur_sigma >= 0.0f && std::isfinite(d.blur_sigma), "plan_create: bad blur");
+  emc_plan* p = new emc_plan();
+  p->ctx = ctx;
+  p->d = d;
+  p->n2 = d.side * d.side;
+  p->Np = ceil_div(d.n_images, 128) * 128;
+  p->Rp = ceil_div(d.n_rot, 128) * 128;
+  p->n_rt = ceil_div(d.n_rot, EMC_RT);
+  const size_t RN = (size_t)d.n_rot * d.n_images;
+  const size_t n3 = (size_t)d.side * d.side * d.side;
+  int rc = EMC_OK;
+  if (!rc) rc = alloc_n(p, &p->L, RN);
+  if (!rc) rc = alloc_n(p, &p->PHI, RN);
+  if (!rc) rc = alloc_n(p, &p->part, (size_t)p->n_rt * d.n_images);
+  if (!rc) rc = alloc_n(p, &p->lse, d.n_images);
+  if (!rc) rc = alloc_n(p, &p->T, p->Rp);
+  if (!rc) rc = alloc_n(p, &p->rot_cnt, p->Rp);
+  if (!rc) rc = alloc_n(p, &p->rot_A, p->Rp);
+  if (!rc) rc = alloc_n(p, &p->rot_ssum, p->Rp);
+  if (!rc) rc = alloc_n(p, &p->red, (size_t)kRedSlots + 2 * (size_t)p->Rp + 2 * 1024 + 2);
+  if (!rc) rc = alloc_n(p, &p->cnorm, d.n_images);
+  if (!rc) rc = alloc_n(p, &p->Ksum, d.n_images);
+  if (!rc) rc = alloc_n(p, &p->flags, 16);
+  if (!rc && d.precision == EMC_PREC_FP32) rc = alloc_n(p, &p->Q, (size_t)d.n_rot * p->Np);
+  if (!rc && d.insert_mode == EMC_INSERT_DETERMINISTIC) {
+    rc = alloc_n(p, &p->fix_m, n3);
+    if (!rc) rc = alloc_n(p, &p->fix_w, n3);
+  }
+  if (rc) {
+    emc_plan_destroy(p);
+    return rc;
+  }
+  *out = p;
+  return EMC_OK;
+}
+
+extern "C" int emc_plan_destroy(emc_plan* p) {
+  if (!p) return EMC_OK;
+  if (p->ctx) cudaStreamSynchronize(p->ctx->stream);
+  for (void* a : p->allocs) cudaFree(a);
+  delete p;
+  return EMC_OK;
+}
+
+extern "C" size_t emc_plan_workspace_bytes(const emc_plan* p) { return p ? p->bytes : 0; }
+
+extern "C" int emc_plan_bind(emc_plan* p, const float* d_images, const int* d_mask,
+                             const float* d_x, const float* d_y, const float* d_z,
+                             const float* d_rot, const float* d_rot_weights) {
+  if (!p) return EMC_ERR_INVALID;
+  emc_ctx* ctx = p->ctx;
+  EMC_REQUIRE(ctx, d_images && d_mask && d_x && d_y && d_z && d_rot && d_rot_weights,
+              "plan_bind: null pointer");
+  EMC_REQUIRE(ctx, !p->bound, "plan_bind: plan already bound");
+  const int n2 = p->n2, N = p->d.n_images;
+  // Mask -> compacted pixel list (host; once per plan).
+  std::vector<int> hmask(n2);
+  EMC_CUDA(ctx, cudaMemcpyAsync(hmask.data(), d_mask, sizeof(int) * n2, cudaMemcpyDeviceToHost,
+                                ctx->stream));
+  EMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  std::vector<int> pix;
+  for (int q = 0; q < n2; ++q) {
+    EMC_REQUIRE(ctx, hmask[q] == 0 || hmask[q] == 1, "plan_bind: mask values must be 0 or 1");
+    if (hmask[q]) pix.push_back(q);
+  }
+  EMC_REQUIRE(ctx, !pix.empty(), "plan_bind: mask is empty");
+  p->P_eff = (int)pix.size();
+  p->Kp = ceil_div(p->P_eff, 128) * 128;  // whole 128-pixel M-step tiles
+  pix.resize(p->Kp, -1);
+  int rc = EMC_OK;
+  if (!rc) rc = alloc_n(p, &p->pix, p->Kp);
+  if (!rc) rc = alloc_n(p, &p->cx, p->Kp);
+  if (!rc) rc = alloc_n(p, &p->cy, p->Kp);
+  if (!rc) rc = alloc_n(p, &p->cz, p->Kp);
+  if (!rc) rc = alloc_n(p, &p->Kraw, (size_t)N * p->Kp);
+  if (!rc) rc = alloc_n(p, &p->S, (size_t)p->Rp * p->Kp);
+  if (!rc && p->d.precision == EMC_PREC_FP32) {
+    rc = alloc_n(p, &p->Kt, (size_t)N * p->Kp);
+    if (!rc) rc = alloc_n(p, &p->K2, (size_t)N * p->Kp);
+  }
+  if (rc) return rc;
+  EMC_CUDA(ctx, cudaMemcpyAsync(p->pix, pix.data(), sizeof(int) * p->Kp, cudaMemcpyHostToDevice,
+                                ctx->stream));
+  EMC_CUDA(ctx, cudaMemsetAsync(p->flags, 0, 16 * sizeof(int), ctx->stream));
+  EMC_CUDA(ctx, cudaMemsetAsync(p->S, 0, sizeof(float) * (size_t)p->Rp * p->Kp, ctx->stream));
+  gather_coords_kernel<<<ceil_div(p->Kp, 256), 256, 0, ctx->stream>>>(p->pix, d_x, d_y, d_z, p->cx,
+                                                                      p->cy, p->cz, p->Kp);
+  if ((rc = after_launch(ctx, "gather_coords_kernel"))) return rc;
+  pattern_norm_kernel<<<ceil_div(N, 128), 128, 0, ctx->stream>>>(d_images, d_mask, n2, N,
+                                                                 p->d.normalize_images, p->cnorm);
+  if ((rc = after_launch(ctx, "pattern_norm_kernel"))) return rc;
+  // Kt / K2 exist only for the FP32 path (null: not written).
+  pattern_ops_kernel<<<dim3(ceil_div(p->Kp, 256), N), 256, 0, ctx->stream>>>(
+      d_images, p->pix, p->cnorm, n2, N, p->Kp, p->Kraw, p->Kt, p->K2, p->flags);
+  if ((rc = after_launch(ctx, "pattern_ops_kernel"))) return rc;
+  row_sum_kernel<<<N, 256, 0, ctx->stream>>>(p->Kraw, p->Kp, p->Kp, p->Ksum);
+  if ((rc = after_launch(ctx, "row_sum_kernel"))) return rc;
+  int hflags[16];
+  EMC_CUDA(ctx, cudaMemcpyAsync(hflags, p->flags, sizeof(hflags), cudaMemcpyDeviceToHost, ctx->stream));
+  EMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  if (hflags[0] & 1) return fail(ctx, EMC_ERR_NONFINITE, "plan_bind: images contain NaN/Inf");
+  p->counts_fp16_exact = !(hflags[0] & 2);
+  p->images = d_images;
+  p->mask = d_mask;
+  p->x = d_x;
+  p->y = d_y;
+  p->z = d_z;
+  p->rot = d_rot;
+  p->rotw = d_rot_weights;
+  if (p->d.precision == EMC_PREC_MIXED) {
+    if ((rc = tc_bind(p))) return rc;
+  }
+  p->bound = true;
+  return EMC_OK;
+}
+
+static int plan_expand(emc_plan* p, const float* model) {
+  emc_ctx* ctx = p->ctx;
+  if (p->d.interp == EMC_INTERP_NEAREST)
+    slice_rows_kernel<EMC_INTERP_NEAREST><<<p->d.n_rot, 256, 0, ctx->stream>>>(
+        model, p->d.side, p->rot, p->pix, p->cx, p->cy, p->cz, p->d.n_rot, p->Kp, p->S,
+        p->rot_cnt, p->rot_A, p->rot_ssum);
+  else
+    slice_rows_kernel<EMC_INTERP_TRILINEAR><<<p->d.n_rot, 256, 0, ctx->stream>>>(
+        model, p->d.side, p->rot, p->pix, p->cx, p->cy, p->cz, p->d.n_rot, p->Kp, p->S,
+        p->rot_cnt, p->rot_A, p->rot_ssum);
+  return after_launch(ctx, "slice_rows_kernel");
+}
+
+static int plan_estep_fp32(emc_plan* p, float sigma) {
+  emc_ctx* ctx = p->ctx;
+  EstepArgs a;
+  a.S = p->S;
+  a.Kraw = p->Kraw;
+  a.Kt = p->Kt;
+  a.K2 = p->K2;
+  a.Ksum = p->Ksum;
+  a.rot_cnt = p->rot_cnt;
+  a.rot_ssum = p->rot_ssum;
+  a.rotw = p->rotw;
+  a.L = p->L;
+  a.PHI = p->PHI;
+  a.part = p->part;
+  a.bad = p->flags + 4;
+  a.R = p->d.n_rot;
+  a.N = p->d.n_images;
+  a.Kp = p->Kp;
+  a.inv2s2 = 1.0f / (2.0f * sigma * sigma);
+  a.known_intensity = p->d.known_intensity;
+  dim3 grid(ceil_div(a.N, BN), ceil_div(a.R, BM));
+  if (p->d.diff == EMC_DIFF_POISSON)
+    estep_fp32_kernel<<<grid, TPB, 0, ctx->stream>>>(a);
+  else
+    estep_pois_fp32_kernel<<<grid, TPB, 0, ctx->stream>>>(a);
+  return after_launch(ctx, "estep_fp32_kernel");
+}
+
+static InsertCtx make_insert_ctx(emc_plan* p, float* model, float* weight, double bm, double bw) {
+  InsertCtx c;
+  c.model = model;
+  c.weight = weight;
+  c.fix_m = p->fix_m;
+  c.fix_w = p->fix_w;
+  c.side = p->d.side;
+  c.interp = p->d.interp;
+  c.deterministic = p->d.insert_mode == EMC_INSERT_DETERMINISTIC;
+  // 2^61 / bound: no partial sum can exceed 2^61 < 2^63.
+  c.scale_m = bm > 0 ? std::ldexp(1.0, 61) / bm : 1.0;
+  c.scale_w = bw > 0 ? std::ldexp(1.0, 61) / bw : 1.0;
+  return c;
+}
+
+namespace emc {
+// Inserted-mass bounds of the deterministic mode (host, after mprep).
+int plan_insert_bounds(emc_plan* p, double* bm, double* bw) {
+  emc_ctx* ctx = p->ctx;
+  const int R = p->d.n_rot;
+  std::vector<double> h(2 * (size_t)R);
+  double* row_mass = p->red + kRedSlots;
+  double* row_bound = row_mass + p->Rp;
+  EMC_CUDA(ctx, cudaMemcpyAsync(h.data(), row_mass, sizeof(double) * R, cudaMemcpyDeviceToHost,
+                                ctx->stream));
+  EMC_CUDA(ctx, cudaMemcpyAsync(h.data() + R, row_bound, sizeof(double) * R,
+                                cudaMemcpyDeviceToHost, ctx->stream));
+  EMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  double m = 0.0, w = 0.0;
+  for (int r = 0; r < R; ++r) {
+    m += h[R + r];
+    w += h[r];
+  }
+  *bm = 1.25 * m + 1e-30;
+  *bw = 1.25 * w * (double)p->P_eff + 1e-30;
+  return EMC_OK;
+}
+}  // namespace emc
+
+static int plan_mstep_fp32(emc_plan* p, float* model, float* weight, const InsertCtx& ins) {
+  emc_ctx* ctx = p->ctx;
+  MstepArgs a;
+  a.Q = p->Q;
+  a.Kraw = p->Kraw;
+  a.T = p->T;
+  a.rot = p->rot;
+  a.cx = p->cx;
+  a.cy = p->cy;
+  a.cz = p->cz;
+  a.R = p->d.n_rot;
+  a.N = p->d.n_images;
+  a.Kp = p->Kp;
+  a.ldq = p->Np;
+  a.P_eff = p->P_eff;
+  a.ins = ins;
+  (void)model;
+  (void)weight;
+  dim3 grid(ceil_div(p->P_eff, BN), ceil_div(a.R, BM));
+  mstep_fp32_kernel<<<grid, TPB, 0, ctx->stream>>>(a);
+  return after_launch(ctx, "mstep_fp32_kernel");
+}
+
+extern "C" int emc_iterate(emc_plan* p, float* d_model, float* d_weight, float sigma,
+                           emc_iter_stats* stats) {
+  if (!p) return EMC_ERR_INVALID;
+  emc_ctx* ctx = p->ctx;
+  EMC_REQUIRE(ctx, p->bound, "iterate: plan not bound");
+  EMC_REQUIRE(ctx, d_model && d_weight, "iterate: null model/weight");
+  EMC_REQUIRE(ctx, sigma > 0.0f && std::isfinite(sigma), "iterate: bad sigma");
+  const int R = p->d.n_rot, N = p->d.n_images;
+  const long long n3 = (long long)p->d.side * p->d.side * p->d.side;
+  int rc;
+  EMC_CUDA(ctx, cudaMemsetAsync(p->flags + 4, 0, sizeof(int), ctx->stream));
+  // expand
+  if ((rc = plan_expand(p, d_model))) return rc;
+  // scaling + likelihood + per-tile LSE partials
+  if (p->d.precision == EMC_PREC_MIXED)
+    rc = tc_estep(p, sigma);
+  else
+    rc = plan_estep_fp32(p, sigma);
+  if (rc) return rc;
+  // normaliser
+  lse_combine_kernel<<<ceil_div(N, 256), 256, 0, ctx->stream>>>(p->part, p->n_rt, N, p->lse);
+  if ((rc = after_launch(ctx, "lse_combine_kernel"))) return rc;
+  finite_sum_kernel<<<1, 256, 0, ctx->stream>>>(p->lse, N, p->red + kRedLL);
+  if ((rc = after_launch(ctx, "finite_sum_kernel"))) return rc;
+  double* row_mass = p->red + kRedSlots;
+  double* row_bound = row_mass + p->Rp;
+  mprep_kernel<<<R, 256, 0, ctx->stream>>>(p->L, p->PHI, p->lse, p->Ksum, R, N,
+                                            p->d.precision == EMC_PREC_FP32 ? p->Q : nullptr,
+                                            p->Np, p->T, row_mass, row_bound);
+  if ((rc = after_launch(ctx, "mprep_kernel"))) return rc;
+  // M-step into zeroed accumulators
+  double bm = 0.0, bw = 0.0;
+  const bool det = p->d.insert_mode == EMC_INSERT_DETERMINISTIC;
+  if (det) {
+    if ((rc = plan_insert_bounds(p, &bm, &bw))) return rc;
+    EMC_CUDA(ctx, cudaMemsetAsync(p->fix_m, 0, sizeof(unsigned long long) * n3, ctx->stream));
+    EMC_CUDA(ctx, cudaMemsetAsync(p->fix_w, 0, sizeof(unsigned long long) * n3, ctx->stream));
+  } else {
+    EMC_CUDA(ctx, cudaMemsetAsync(d_model, 0, sizeof(float) * n3, ctx->stream));
+    EMC_CUDA(ctx, cudaMemsetAsync(d_weight, 0, sizeof(float) * n3, ctx->stream));
+  }
+  InsertCtx ins = make_insert_ctx(p, d_model, d_weight, bm, bw);
+  if (p->d.precision == EMC_PREC_MIXED)
+    rc = tc_mstep(p, d_model, d_weight);
+  else
+    rc = plan_mstep_fp32(p, d_model, d_weight, ins);
+  if (rc) return rc;
+  if (det) {
+    const int nb = (int)std::min<long long>(ceil_div(n3, 256), (long long)ctx->sm_count * 8);
+    fixed_to_model_kernel<<<nb, 256, 0, ctx->stream>>>(p->fix_m, p->fix_w, 1.0 / ins.scale_m,
+                                                        1.0 / ins.scale_w, d_model, d_weight, n3);
+    if ((rc = after_launch(ctx, "fixed_to_model_kernel"))) return rc;
+  }
+  // divide, normalise, blur
+  if ((rc = launch_divide_by_weight(ctx, d_model, d_weight, n3))) return rc;
+  double* mean_stats = p->red + kRedMean;
+  // launch_positive_mean writes {sum, count} then its partials after them;
+  // kRedMean + 2 + 2*1024 fits in the reduction buffer tail.
+  double* tail = p->red + kRedSlots + 2 * (size_t)p->Rp;
+  if ((rc = launch_positive_mean(ctx, d_model, n3, tail))) return rc;
+  EMC_CUDA(ctx, cudaMemcpyAsync(mean_stats, tail, 2 * sizeof(double), cudaMemcpyDeviceToDevice,
+                                ctx->stream));
+  if ((rc = launch_scale_by_inverse_mean(ctx, d_model, n3, tail))) return rc;
+  if (p->d.blur_sigma > 0.0f) {
+    if ((rc = launch_blur(ctx, d_model, p->d.side, p->d.blur_sigma))) return rc;
+  }
+  if (stats) {
+    double h[kRedSlots];
+    int bad = 0;
+    std::vector<double> mass(R);
+    EMC_CUDA(ctx, cudaMemcpyAsync(h, p->red, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
+    EMC_CUDA(ctx, cudaMemcpyAsync(mass.data(), row_mass, sizeof(double) * R,
+                                  cudaMemcpyDeviceToHost, ctx->stream));
+    EMC_CUDA(ctx, cudaMemcpyAsync(&bad, p->flags + 4, sizeof(int), cudaMemcpyDeviceToHost,
+                                  ctx->stream));
+    EMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    double m = 0.0;
+    for (double v : mass) m += v;
+    stats->total_loglik = h[kRedLL];
+    stats->model_mean_before = h[kRedMean + 1] > 0 ? h[kRedMean] / h[kRedMean + 1] : 0.0;
+    stats->captured_mass = m / (double)N;
+    stats->bad_pairs = bad;
+    stats->reserved = 0;
+  }
+  return EMC_OK;
+}
+
+extern "C" int emc_plan_results(emc_plan* p, const float** d_respons, const float** d_scaling,
+                                const double** d_lse) {
+  if (!p) return EMC_ERR_INVALID;
+  if (d_respons) *d_respons = p->L;
+  if (d_scaling) *d_scaling = p->PHI;
+  if (d_lse) *d_lse = p->lse;
+  return EMC_OK;
+}

@@ -1,0 +1,95 @@
+// The fused-iteration plan: workspace layout and kernels shared by the FP32
+// and tensor-core paths.
+#pragma once
+#include <cuda_fp16.h>
+
+#include <vector>
+
+#include "common.cuh"
+
+// Rotations per E-step tile; LSE partials are kept per tile of this many rows.
+#define EMC_RT 128
+
+struct emc_plan {
+  emc_ctx* ctx = nullptr;
+  emc_plan_desc d{};
+  int n2 = 0;      // side*side
+  int P_eff = 0;   // pixels with mask != 0
+  int Kp = 0;      // P_eff padded (128)
+  int Np = 0;      // patterns padded (128)
+  int Rp = 0;      // rotations padded (128)
+  int n_rt = 0;    // rotation tiles of EMC_RT
+  bool bound = false;
+  bool counts_fp16_exact = false;  // every count is an integer in [0, 2048]
+
+  // bound inputs (caller owned)
+  const float* images = nullptr;
+  const int* mask = nullptr;
+  const float *x = nullptr, *y = nullptr, *z = nullptr;
+  const float* rot = nullptr;
+  const float* rotw = nullptr;
+
+  // compacted geometry
+  int* pix = nullptr;                          // [Kp], -1 padding
+  float *cx = nullptr, *cy = nullptr, *cz = nullptr;  // [Kp]
+
+  // pattern operands, rows of Kp (FP32 path)
+  float* Kraw = nullptr;  // k (x c_i when normalising)
+  float* Kt = nullptr;    // k if k > 1e-10 else 0
+  float* K2 = nullptr;    // Kt^2
+  float* Ksum = nullptr;  // [N] sum_p k
+  float* cnorm = nullptr; // [N] c_i (1 when not normalising)
+
+  // pattern operands (tensor-core path): counts as FP16, rows of Kp
+  __half* Kh = nullptr;      // k
+  __half* K2hi = nullptr;    // fp16(k^2 * 2^-e)
+  __half* K2lo = nullptr;    // k^2 * 2^-e - K2hi
+  unsigned char* k2lo_any = nullptr;  // [Np/128][Kp/32] block has a nonzero K2lo
+  __half* KhT = nullptr;     // [Kp][Np] transposed counts for the M-step
+
+  // rotation side, per iteration
+  float* S = nullptr;       // [Rp][Kp] slice at the compacted pixels (FP32 path)
+  float* rot_cnt = nullptr; // [Rp] count_r (pixels with s > 0)
+  float* rot_A = nullptr;   // [Rp] sum s^2/(s+c) over s > 0
+  float* rot_ssum = nullptr;// [Rp] sum max(s, floor) (true Poisson)
+  __half* Gop = nullptr;    // [6][Rp][Kp] rotation operands (tensor-core path)
+
+  // responsibilities
+  float* L = nullptr;      // [R][N] log-likelihood, then normalised responsibility
+  float* PHI = nullptr;    // [R][N] scaling
+  float* Q = nullptr;      // [R][N] responsibility / scaling (FP32 M-step)
+  __half* Qh = nullptr;    // [Rp][Np] hi (tensor-core M-step)
+  __half* Ql = nullptr;    // [Rp][Np] lo
+  float2* part = nullptr;  // [n_rt][N] (max, sumexp) per rotation tile
+  double* lse = nullptr;   // [N]
+  float* T = nullptr;      // [Rp] rotation totals
+  double* red = nullptr;   // reduction scratch (small)
+  unsigned long long* fix_m = nullptr;  // [s^3] fixed-point model (deterministic insert)
+  unsigned long long* fix_w = nullptr;
+  int* flags = nullptr;    // device status words
+
+  std::vector<void*> allocs;
+  size_t bytes = 0;
+};
+
+namespace emc {
+
+// Voxel-sum upper bound and fixed-point scale slots in plan->red.
+enum RedSlot {
+  kRedLL = 0,        // total log-likelihood
+  kRedMass = 1,      // captured responsibility mass
+  kRedBad = 2,       // invalid pairs
+  kRedBoundM = 3,    // upper bound of inserted model mass
+  kRedBoundW = 4,    // upper bound of inserted weight
+  kRedMean = 5,      // {sum, count} of positive voxels (2 slots) + partials
+  kRedSlots = 8,
+};
+
+int plan_alloc(emc_plan* p, void** ptr, size_t bytes);
+
+// Tensor-core path (tc_gemm.cu).
+int tc_bind(emc_plan* p);
+int tc_estep(emc_plan* p, float sigma);
+int tc_mstep(emc_plan* p, float* model, float* weight);
+
+}  // namespace emc

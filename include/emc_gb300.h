@@ -1,0 +1,236 @@
+/*
+ * emc_gb300.h -- C ABI of the GB300 (sm_103a) EMC iteration.
+ *
+ * The per-function entry points below replace the C++-linkage `cuda_*`
+ * functions of the reference (emc_cuda_help.h:9-117) one for one.  The
+ * reference passes spimage structs only to carry sizes; here the sizes are
+ * plain ints.  Every buffer argument is a raw device pointer owned by the
+ * caller, laid out exactly as in the reference:
+ *
+ *   model, weight    float[side*side*side]     index z*side*side + y*side + x
+ *   slices           float[chunk*N_2d]         index r*N_2d + p,  p = y*side + x
+ *   images           float[N_images*N_2d]      index i*N_2d + p
+ *   mask             int[N_2d]                 common detector mask
+ *   respons, scaling float[n_slices*N_images]  rotation-major: r*N_images + i
+ *   rotations        float[4*R]                unit quaternions (w, x, y, z)
+ *   x/y/z coords     float[N_2d]               detector pixel -> reciprocal space
+ *
+ * Conventions that differ from the reference (boundary rows B2-B4 of the
+ * design): every function returns an int status (EMC_OK == 0, negative on
+ * error) and never prints; the text of the last error is kept per context
+ * (emc_last_error).  Work is queued on the context's stream and is
+ * asynchronous unless a function returns a host value; emc_sync() waits.
+ * A context is not re-entrant: one host thread drives it at a time.
+ */
+#ifndef EMC_GB300_H
+#define EMC_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define EMC_OK 0
+#define EMC_ERR_INVALID (-1)     /* bad argument (null pointer, size, enum)      */
+#define EMC_ERR_CUDA (-2)        /* a CUDA runtime call failed                   */
+#define EMC_ERR_TIMEOUT (-3)     /* a bounded device-side wait gave up           */
+#define EMC_ERR_NONFINITE (-4)   /* NaN/Inf detected where the contract forbids  */
+#define EMC_ERR_INTERNAL (-5)    /* invariant violated (a bug)                   */
+#define EMC_ERR_NOMEM (-6)       /* device allocation failed                     */
+#define EMC_ERR_UNSUPPORTED (-7) /* input outside what the chosen path handles   */
+
+/* ---- enums ------------------------------------------------------------- */
+/* diff_type of the reference (configs.h:11). */
+#define EMC_DIFF_ABSOLUTE 0
+#define EMC_DIFF_POISSON 1  /* the reference's "poisson": weighted least squares */
+#define EMC_DIFF_RELATIVE 2
+#define EMC_DIFF_TRUE_POISSON 3 /* new: counts x log(slice) Poisson likelihood  */
+
+/* slice interpolation */
+#define EMC_INTERP_NEAREST 0   /* reference: lroundf to the nearest voxel */
+#define EMC_INTERP_TRILINEAR 1 /* new: trilinear gather / splat           */
+
+/* arithmetic of the fused iteration (emc_plan_*) */
+#define EMC_PREC_FP32 0  /* plain FP32 SIMT kernels                         */
+#define EMC_PREC_MIXED 1 /* FP16 tensor-core GEMMs, hi+lo split, FP32 accum */
+
+/* model insertion of the fused iteration */
+#define EMC_INSERT_ATOMIC 0        /* float atomics (order-dependent rounding) */
+#define EMC_INSERT_DETERMINISTIC 1 /* order-independent: bit-identical reruns  */
+
+typedef struct emc_ctx emc_ctx;
+typedef struct emc_plan emc_plan;
+
+/* ---- context ----------------------------------------------------------- */
+/* Replaces cuda_set_device (emc_cuda.cu:867-870; main.cpp:127): binds the
+ * context to `device` and creates its stream. */
+int emc_ctx_create(emc_ctx** out, int device);
+int emc_ctx_destroy(emc_ctx* ctx);
+/* Text of the last error on this context (never NULL). */
+const char* emc_last_error(const emc_ctx* ctx);
+/* Use an external cudaStream_t (NULL: the context's own stream). */
+int emc_set_stream(emc_ctx* ctx, void* cuda_stream);
+void* emc_get_stream(const emc_ctx* ctx);
+int emc_sync(emc_ctx* ctx);
+/* Number of kernels this context launched since creation (instrumentation). */
+long long emc_kernel_launches(const emc_ctx* ctx);
+
+/* ---- host inputs ------------------------------------------------------- */
+/* rotations.c:43 n_to_samples(n)/2: rotations kept for sampling level n. */
+int emc_rotation_count(int n);
+/* rotations.c:77-458 generate_rotation_list: 600-cell sampling at level n,
+ * q0>0 hemisphere, weights normalised by their float sum.  Writes 4*R floats
+ * to quats and R floats to weights (host memory).  Returns R or < 0. */
+int emc_generate_rotations(int n, float* quats, float* weights, int capacity);
+/* emc_helper.cpp:55-79 calculate_coordinates: Ewald-sphere coordinates of the
+ * side x side detector, written as [y*side + x] (host memory). */
+int emc_calculate_coordinates(int side, float pixel_size, float detector_distance,
+                              float wavelength, float* x, float* y, float* z);
+/* main.cpp:251: sigma_t = sf + (ss - sf) * exp(-t / half_life * ln 2). */
+float emc_sigma_schedule(int iteration, double sigma_start, double sigma_final, int half_life);
+
+/* ---- per-function drop-ins (reference semantics) ----------------------- */
+/* cuda_get_slices (emc_cuda_help.h:47-49; emc_cuda.cu:102-157, 542-560):
+ * slices[r] for rotations start_slice .. start_slice+slice_chunk-1 of d_rot.
+ * EMC_INTERP_NEAREST reproduces the reference bit for bit (out-of-volume
+ * pixels get -1); EMC_INTERP_TRILINEAR is the new gather. */
+int emc_get_slices(emc_ctx* ctx, const float* d_model, int side, float* d_slices,
+                   const float* d_rot, const float* d_x, const float* d_y, const float* d_z,
+                   int start_slice, int slice_chunk, int interp);
+
+/* cuda_update_scaling_full (emc_cuda_help.h:36-37; emc_cuda.cu:438-454,
+ * 516-539): scaling[(start+r)*N_images + i] = sum k^2 / sum k*s over mask>0,
+ * s>1e-10, k>1e-10, with the reference's int-truncated denominator. */
+int emc_update_scaling_full(emc_ctx* ctx, const float* d_images, const float* d_slices,
+                            const int* d_mask, float* d_scaling, int N_2d, int N_images,
+                            int slice_start, int slice_chunk, int diff);
+
+/* cuda_calculate_responsabilities (emc_cuda_help.h:40-43; emc_cuda.cu:159-295):
+ * respons[(start+r)*N_images + i] = log(w[start+r]) - S / (2 count sigma^2),
+ * S the per-pixel difference sum of `diff` (FP64 per pixel for POISSON, as
+ * in the reference). */
+int emc_calculate_responsabilities(emc_ctx* ctx, const float* d_slices, const float* d_images,
+                                   const int* d_mask, float sigma, const float* d_scaling,
+                                   float* d_respons, const float* d_weights, int N_2d,
+                                   int N_images, int slice_start, int slice_chunk, int diff);
+
+/* cuda_max_vector (emc_cuda_help.h:117; emc_cuda.cu:1041-1056, 1136-1145):
+ * maxr[i] = max(-1e10, max_r respons[r*N_images + i]). */
+int emc_max_vector(emc_ctx* ctx, const float* d_respons, int N_images, int n_slices,
+                   float* d_maxr);
+
+/* cuda_respons_max_expf (emc_cuda_help.h:85-86; emc_cuda.cu:1175-1217):
+ * sum[i] = sum_r expf(respons - max[i]) over terms with respons-max > -1e10.
+ * Unlike the reference, respons is not modified and nothing is allocated. */
+int emc_respons_max_expf(emc_ctx* ctx, const float* d_respons, const float* d_max,
+                         int N_images, int n_slices, float* d_sum);
+
+/* cuda_norm_respons_sumexpf (emc_cuda_help.h:89; emc_cuda.cu:1253-1272):
+ * respons = expf(respons - lse[i]) in place; lse = log(sum) + max is formed
+ * by the caller (main.cpp:384-391) and passed as d_sum. */
+int emc_norm_respons_sumexpf(emc_ctx* ctx, float* d_respons, const float* d_sum,
+                             const float* d_max, int N_images, int n_slices);
+
+/* Convenience for the host step between the two calls above
+ * (emc_helper.cpp:579-587 log_vector + sum_vectors, float):
+ * lse[i] = logf(sum[i]) + max[i], on the device. */
+int emc_log_sum_max(emc_ctx* ctx, const float* d_sum, const float* d_max, float* d_lse,
+                    int N_images);
+
+/* cuda_update_slices (emc_cuda_help.h:10-16; emc_cuda.cu:562-594;
+ * emc_atomic.cu:33-132, 183-200): M-step slice average over active images
+ * for rotations start..start+chunk-1 written to d_slices[0..chunk), then
+ * nearest-voxel insertion of the chunk into d_model / d_weight with
+ * weight T_r = sum_i respons.  d_rot points at the chunk's first quaternion
+ * (the reference passes &d_rotations[start*4], main.cpp:458). */
+int emc_update_slices(emc_ctx* ctx, const float* d_images, float* d_slices, const int* d_mask,
+                      const float* d_respons, const float* d_scaling, const int* d_active_images,
+                      int N_images, int slice_start, int slice_chunk, int N_2d, int side,
+                      float* d_model, const float* d_x, const float* d_y, const float* d_z,
+                      const float* d_rot, float* d_weight);
+
+/* cuda_divide_model_by_weight (emc_cuda_help.h:60; emc_cuda.cu:758-786):
+ * model /= weight where weight > 0, else -1. */
+int emc_divide_model_by_weight(emc_ctx* ctx, int side, float* d_model, const float* d_weight);
+
+/* cuda_normalize_model (emc_cuda_help.h:61; emc_cuda.cu:639-671, 788-798):
+ * model *= 1/mean(model > 0).  Writes the mean before scaling to *h_mean
+ * when h_mean is not NULL (synchronises). */
+int emc_normalize_model(emc_ctx* ctx, int side, float* d_model, float* h_mean);
+
+/* cuda_model_max / cuda_model_average (emc_cuda.cu:629-671): diagnostics,
+ * synchronous, result in host memory. */
+int emc_model_max(emc_ctx* ctx, const float* d_model, int n, float* h_out);
+int emc_model_average(emc_ctx* ctx, const float* d_model, int n, float* h_out);
+
+/* cuda_blur_model (emc_cuda_help.h:116; emc_cuda.cu:1404-1492): the
+ * reference's intent (its FFT calls are commented out) -- negative voxels are
+ * masked, the rest convolved with a periodic Gaussian of std `sigma` voxels,
+ * masked voxels restored to -1.  Separable shared-memory stencil. */
+int emc_blur_model(emc_ctx* ctx, float* d_model, int side, float sigma);
+
+/* cuda_reset_real / cuda_reset_model (emc_cuda_help.h:9, 56). */
+int emc_reset_real(emc_ctx* ctx, float* d_real, int len);
+
+/* cuda_copy_real_to_device / cuda_copy_real_to_host / cuda_copy_real_d2d
+ * (emc_cuda_help.h:92-97; emc_cuda.cu:885-911): n floats, synchronous with
+ * respect to the host for the *_to_host form; d2d copies into dst[start..). */
+int emc_copy_real_to_device(emc_ctx* ctx, const float* h_src, float* d_dst, int n);
+int emc_copy_real_to_host(emc_ctx* ctx, float* h_dst, const float* d_src, int n);
+int emc_copy_real_d2d(emc_ctx* ctx, float* d_dst, const float* d_src, int start, int n);
+
+/* ---- fused iteration (the fast path) ----------------------------------- */
+typedef struct {
+  int side;            /* model side s; detector is s x s                      */
+  int n_images;        /* N                                                    */
+  int n_rot;           /* R                                                    */
+  int diff;            /* EMC_DIFF_POISSON (reference) or EMC_DIFF_TRUE_POISSON */
+  int interp;          /* EMC_INTERP_*                                          */
+  int precision;       /* EMC_PREC_*                                            */
+  int insert_mode;     /* EMC_INSERT_*                                          */
+  int known_intensity; /* 1: skip scaling (phi = 1), as known_intensity=1       */
+  int normalize_images;/* 1: fold the reference's per-pattern normalisation     */
+  float blur_sigma;    /* > 0: blur the model after normalisation               */
+} emc_plan_desc;
+
+typedef struct {
+  double total_loglik;       /* sum_i lse_i (FP64)                              */
+  double model_mean_before;  /* mean(model > 0) before normalisation            */
+  double captured_mass;      /* sum of responsibilities / N (== 1 when full)    */
+  int bad_pairs;             /* pairs with undefined scaling or empty overlap   */
+  int reserved;
+} emc_iter_stats;
+
+/* Creates a plan: validates the description and allocates the workspace
+ * (slice operands, responsibilities, scaling, LSE partials) once. */
+int emc_plan_create(emc_ctx* ctx, const emc_plan_desc* desc, emc_plan** out);
+int emc_plan_destroy(emc_plan* plan);
+/* Bytes of device workspace the plan holds. */
+size_t emc_plan_workspace_bytes(const emc_plan* plan);
+/* Binds the problem's device inputs (caller-owned, must outlive the plan's
+ * use) and pre-processes the patterns (FP16 count operands, compaction to
+ * the masked pixels).  images [N*s*s], mask [s*s], coords [s*s] x3,
+ * rotations [4R], rotation weights [R]. */
+int emc_plan_bind(emc_plan* plan, const float* d_images, const int* d_mask, const float* d_x,
+                  const float* d_y, const float* d_z, const float* d_rot,
+                  const float* d_rot_weights);
+/* One EMC iteration: expand, scaling, likelihood, log-sum-exp, M-step,
+ * insertion, divide, normalise (+ blur).  d_model is read and overwritten
+ * with the new normalised model; d_weight receives the insertion weights.
+ * stats (host, may be NULL) is filled after a synchronise. */
+int emc_iterate(emc_plan* plan, float* d_model, float* d_weight, float sigma,
+                emc_iter_stats* stats);
+/* Device pointers into the plan's workspace (valid until the next call):
+ * the normalised responsibilities [R*N] (rotation-major) and scaling [R*N]
+ * of the last iteration, and the per-pattern lse [N] (double). */
+int emc_plan_results(emc_plan* plan, const float** d_respons, const float** d_scaling,
+                     const double** d_lse);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* EMC_GB300_H */

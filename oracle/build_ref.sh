@@ -1,0 +1,51 @@
+#!/usr/bin/env bash
+# Builds the reference's own code for use as a checker, from the reference
+# sources where they lie (never copied into the repository):
+#   oracle/_ref/ref_rotations          rotations.c + a KAT driver (host, any CPU)
+#   oracle/_ref/libemc_ref_kernels.so  emc_cuda.cu + emc_atomic.cu for sm_103a,
+#                                      behind the C wrappers of ref_harness.cu
+#                                      (only with --kernels; needs nvcc)
+# The reference tree is $EMC_REF_DIR, else /root/reference, else the staged
+# copy baseline/_ref/src (git-ignored; see --stage).  Outputs go to
+# oracle/_ref/ only.
+#   --stage   copy the reference files the kernels need into baseline/_ref/src
+#             (git-ignored) so that a GPU machine without the reference tree can
+#             build the kernel harness.
+set -euo pipefail
+here="$(cd "$(dirname "$0")" && pwd)"
+repo="$(cd "$here/.." && pwd)"
+out="$here/_ref"
+ref="${EMC_REF_DIR:-}"
+if [[ -z "$ref" ]]; then
+  if [[ -d /root/reference ]]; then ref=/root/reference; else ref="$repo/baseline/_ref/src"; fi
+fi
+want_kernels=0
+for a in "$@"; do
+  case "$a" in
+    --kernels) want_kernels=1 ;;
+    --stage)
+      mkdir -p "$repo/baseline/_ref/src"
+      for f in rotations.c rotations.h emc_cuda.cu emc_atomic.cu emc_cuda_help.h emc_helper.h configs.h; do
+        cp "$ref/$f" "$repo/baseline/_ref/src/$f"
+      done
+      echo "staged reference sources in baseline/_ref/src"
+      exit 0 ;;
+  esac
+done
+if [[ ! -f "$ref/rotations.c" ]]; then
+  echo "reference tree not found ($ref)" >&2
+  exit 1
+fi
+mkdir -p "$out"
+gcc -O2 -std=gnu99 -w -I"$here/shim" -I"$ref" -include stdio.h -include stdlib.h \
+    -include string.h -include math.h \
+    "$ref/rotations.c" "$here/ref_rotations_main.c" "$here/shim/spimage_stubs.c" -lm \
+    -o "$out/ref_rotations"
+if [[ $want_kernels == 1 ]]; then
+  nvcc -std=c++17 -O3 -gencode arch=compute_103a,code=sm_103a -Xcompiler -fPIC -shared -w \
+      -I"$here/shim" -I"$ref" -DcudaThreadSynchronize=cudaDeviceSynchronize \
+      -include thrust/transform_reduce.h \
+      "$here/ref_harness.cu" "$here/shim/spimage_stubs.c" -lcufft \
+      -o "$out/libemc_ref_kernels.so"
+fi
+echo "built reference checker in $out"

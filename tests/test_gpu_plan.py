@@ -1,0 +1,154 @@
+"""Parity of the fused iteration (emc_plan_* / emc_iterate) against the FP64
+oracle of its semantics, plus its properties at larger sizes.
+
+Tolerances (FP32 path vs FP64): model relative L2 1e-4, total log-likelihood
+relative 1e-5, responsibilities absolute 1e-4, scaling relative 1e-5."""
+import numpy as np
+import pytest
+import torch
+
+import emc_gb300 as E
+from emc_gb300 import synthetic as S
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def T(a, dev, dt=torch.float32):
+    return torch.as_tensor(np.ascontiguousarray(a), dtype=dt, device=dev)
+
+
+def run_plan(ctx, prob, dev, model=None, sigma=0.3, **kw):
+    s, R, N = prob.cfg.side, prob.quats.shape[0], prob.images.shape[0]
+    plan = E.Plan(ctx, s, N, R, **kw)
+    plan.bind(T(prob.images, dev), T(prob.mask, dev, torch.int32), T(prob.x, dev), T(prob.y, dev),
+              T(prob.z, dev), T(prob.quats, dev), T(prob.weights, dev))
+    m = T(prob.init_model if model is None else model, dev)
+    w = torch.empty_like(m)
+    st = plan.iterate(m, w, sigma)
+    r_ptr, s_ptr, _ = plan.results()
+    resp = ctx.copy_real_to_host(r_ptr, R * N).reshape(R, N)
+    phi = ctx.copy_real_to_host(s_ptr, R * N).reshape(R, N)
+    out = dict(model=m.cpu().numpy().astype(np.float64), weight=w.cpu().numpy().astype(np.float64),
+               respons=resp.astype(np.float64), phi=phi, stats=st)
+    plan.close()
+    return out
+
+
+def rel_l2(a, b):
+    return np.linalg.norm(a - b) / np.linalg.norm(b)
+
+
+CASES = [
+    dict(diff=E.DIFF_POISSON, interp=E.INTERP_NEAREST),
+    dict(diff=E.DIFF_POISSON, interp=E.INTERP_TRILINEAR),
+    dict(diff=E.DIFF_POISSON, interp=E.INTERP_NEAREST, normalize_images=1),
+    dict(diff=E.DIFF_POISSON, interp=E.INTERP_NEAREST, known_intensity=1),
+    dict(diff=E.DIFF_TRUE_POISSON, interp=E.INTERP_NEAREST),
+    dict(diff=E.DIFF_TRUE_POISSON, interp=E.INTERP_TRILINEAR),
+    dict(diff=E.DIFF_POISSON, interp=E.INTERP_NEAREST, blur_sigma=1.0),
+    dict(diff=E.DIFF_POISSON, interp=E.INTERP_NEAREST, insert_mode=E.INSERT_DETERMINISTIC),
+]
+
+
+@pytest.fixture(scope="module")
+def prob():
+    # ragged sizes: N and P_eff not multiples of the 128 tiles
+    return S.make_problem(S.tiny(side=32, n_images=300, rot_n=2, photons=3000, n_atoms=120,
+                                 radius=7.0))
+
+
+@pytest.mark.parametrize("kw", CASES, ids=lambda k: "-".join(f"{a}{b}" for a, b in k.items()))
+def test_fp32_iteration_matches_fp64_oracle(ctx, cuda, prob, kw):
+    sigma = 0.3
+    got = run_plan(ctx, prob, cuda, sigma=sigma, precision=E.PREC_FP32, **kw)
+    want = O.fused_iteration_fp64(prob.init_model, prob.images, prob.mask, prob.x, prob.y, prob.z,
+                                  prob.quats, prob.weights, sigma, prob.cfg.side,
+                                  diff=kw["diff"], interp=kw["interp"],
+                                  known_intensity=bool(kw.get("known_intensity", 0)),
+                                  normalize_images=bool(kw.get("normalize_images", 0)),
+                                  blur_sigma=kw.get("blur_sigma", 0.0))
+    assert rel_l2(got["model"], want["model"]) < 1e-4
+    assert rel_l2(got["weight"], want["weight"]) < 1e-5
+    st = got["stats"]
+    assert abs(st.total_loglik - want["total_loglik"]) <= 1e-5 * abs(want["total_loglik"])
+    assert np.abs(got["respons"] - want["respons"]).max() < 1e-4
+    np.testing.assert_allclose(got["phi"], want["phi"], rtol=1e-5)
+    assert abs(st.captured_mass - 1.0) < 1e-5
+    assert abs(st.model_mean_before - want["mean_before"]) <= 1e-5 * want["mean_before"]
+
+
+def test_deterministic_insert_is_bit_identical(ctx, cuda, prob):
+    a = run_plan(ctx, prob, cuda, insert_mode=E.INSERT_DETERMINISTIC)
+    b = run_plan(ctx, prob, cuda, insert_mode=E.INSERT_DETERMINISTIC)
+    assert np.array_equal(a["model"], b["model"]) and np.array_equal(a["weight"], b["weight"])
+    c = run_plan(ctx, prob, cuda, insert_mode=E.INSERT_ATOMIC)
+    assert rel_l2(a["model"], c["model"]) < 1e-5
+
+
+def test_two_iterations_track_oracle(ctx, cuda, prob):
+    s = prob.cfg.side
+    m = prob.init_model.copy()
+    want = prob.init_model.copy()
+    for it in range(2):
+        sigma = E.sigma_schedule(it, 0.4, 0.12, 25)
+        got = run_plan(ctx, prob, cuda, model=m, sigma=sigma)
+        w = O.fused_iteration_fp64(want, prob.images, prob.mask, prob.x, prob.y, prob.z,
+                                   prob.quats, prob.weights, sigma, s)
+        m = got["model"].astype(np.float32)
+        want = w["model"].astype(np.float32)
+        assert rel_l2(got["model"], w["model"]) < 2e-4
+
+
+def test_zero_photon_pattern_gets_no_responsibility(ctx, cuda, prob):
+    p = S.Problem(**{**prob.__dict__})
+    p.images = prob.images.copy()
+    p.images[7] = 0.0
+    got = run_plan(ctx, p, cuda)
+    assert (got["respons"][:, 7] == 0).all()
+    assert abs(got["stats"].captured_mass - (p.images.shape[0] - 1) / p.images.shape[0]) < 1e-5
+    assert got["stats"].bad_pairs >= p.quats.shape[0]
+
+
+def test_bind_rejects_bad_inputs(ctx, cuda, prob):
+    s, R, N = prob.cfg.side, prob.quats.shape[0], prob.images.shape[0]
+    args = [T(prob.x, cuda), T(prob.y, cuda), T(prob.z, cuda), T(prob.quats, cuda),
+            T(prob.weights, cuda)]
+    bad = prob.images.copy()
+    bad[3, 100] = np.nan
+    plan = E.Plan(ctx, s, N, R)
+    with pytest.raises(E.EmcError, match="NONFINITE"):
+        plan.bind(T(bad, cuda), T(prob.mask, cuda, torch.int32), *args)
+    m2 = prob.mask.copy()
+    m2[0] = 2
+    plan = E.Plan(ctx, s, N, R)
+    with pytest.raises(E.EmcError, match="mask"):
+        plan.bind(T(prob.images, cuda), T(m2, cuda, torch.int32), *args)
+    plan = E.Plan(ctx, s, N, R)
+    m = T(prob.init_model, cuda)
+    with pytest.raises(E.EmcError, match="not bound"):
+        plan.iterate(m, torch.empty_like(m), 0.3)
+    with pytest.raises(E.EmcError):
+        E.Plan(ctx, s, N, R, diff=E.DIFF_ABSOLUTE)
+
+
+def test_properties_at_small_config(ctx, cuda):
+    """The small benchmark configuration (64^3, 2,000 patterns, 3,240
+    rotations): responsibilities normalise per pattern, the model has mean 1
+    over its positive voxels, the weight sums to sum_r T_r x inserted pixels,
+    and deterministic reruns are bit-identical."""
+    prob = S.make_problem(S.CONFIGS["small"], device="cuda")
+    s, R, N = prob.cfg.side, prob.quats.shape[0], prob.images.shape[0]
+    a = run_plan(ctx, prob, cuda, sigma=0.4, insert_mode=E.INSERT_DETERMINISTIC)
+    b = run_plan(ctx, prob, cuda, sigma=0.4, insert_mode=E.INSERT_DETERMINISTIC)
+    assert np.array_equal(a["model"], b["model"])
+    colsum = a["respons"].sum(0)
+    np.testing.assert_allclose(colsum, 1.0, atol=2e-4)
+    pos = a["model"][a["model"] > 0]
+    assert abs(pos.mean() - 1.0) < 1e-5
+    T_r = a["respons"].sum(1)
+    vox = O.nearest_voxels(prob.quats, prob.x[prob.mask == 1], prob.y[prob.mask == 1],
+                           prob.z[prob.mask == 1], s, 0)
+    inserted = (vox >= 0).sum(1)
+    assert abs(a["weight"].sum() - (T_r * inserted).sum()) <= 1e-4 * a["weight"].sum()
+    assert abs(a["stats"].captured_mass - 1.0) < 1e-5

@@ -1,0 +1,426 @@
+#!/usr/bin/env python
+"""EMC iteration throughput on GB300 (one JSON line on rank 0).
+
+Step = one full EMC iteration (expand, scaling, likelihood, log-sum-exp,
+M-step, insertion, divide, normalise) of the mid-size configuration:
+128^3 model, 20,000 patterns of 128x128 (~5,000 photons, scale U(0.5,1.5),
+beamstop 6 px), 25,680 rotations (600-cell level n = 8), the reference's
+"poisson" difference with per-pair scaling.  Synthetic, seeded data with
+those shapes stands in for HDF5 patterns (none are named or available).
+
+value     pairs/s = R * N / step time, inputs resident in HBM, CUDA events on
+          the library's stream around K iterations, max over ranks.
+e2e       the same metric through the public API with host buffers: every
+          step copies the patterns and model from pinned host memory, binds,
+          iterates and reads back model, weight and log-likelihood.
+roofline  the dominant kernel (the E-step: scaling + likelihood + LSE
+          partials), its algorithmic FLOPs per launch over its event-timed
+          duration, against the measured peak in MEASURED_PEAKS.json.
+cpu_baseline / --impl reference
+          the oracle's C restatement of the reference kernels (OpenMP, all
+          host threads) on a bounded sample of the same workload.
+Multi-GPU: replicas only (one independent iteration per rank; the reference's
+rotation split has no exchange to accelerate on single-GPU machines).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "EMC iter/s & rot·pattern pairs/s, mixed-prec+pruned vs plain FP32, same GB300"
+UNIT = "rot·pattern pairs/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--config", default="mid")
+    ap.add_argument("--precision", choices=["auto", "mixed", "fp32"], default="auto")
+    ap.add_argument("--insert", choices=["atomic", "deterministic"], default="atomic")
+    ap.add_argument("--plain-steps", type=int, default=2)
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+# ------------------------------------------------------------ helpers ----
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return dict(hbm=d.get("hbm_gbs"), bf16=d.get("bf16_tflops"),
+                    bf16_sustained=d.get("bf16_tflops_sustained"), source="measured")
+    return dict(hbm=6800.0, bf16=1900.0, bf16_sustained=1700.0, source="fallback")
+
+
+def profile_traffic(kernel_key):
+    """traffic_bytes_per_launch recorded in the committed ncu summary for this
+    kernel and workload (profiles/<kernel>_<workload>.md), else None."""
+    d = os.path.join(ROOT, "profiles")
+    if not os.path.isdir(d):
+        return None
+    for name in sorted(os.listdir(d)):
+        if name.startswith(kernel_key) and name.endswith(".md"):
+            m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", open(os.path.join(d, name)).read())
+            if m:
+                return float(m.group(1))
+    return None
+
+
+REASONS = {  # clocks_event_reasons bit names (nvidia-smi)
+    "hw_slowdown": 0x8, "hw_thermal_slowdown": 0x40, "sw_thermal_slowdown": 0x20,
+    "sw_power_cap": 0x4, "hw_power_brake_slowdown": 0x80,
+}
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed
+    region (started before, stopped after)."""
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+
+    def start(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index),
+                 "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active",
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, mx, reasons = [], [], set()
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 4:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+                bits = int(parts[3], 16)
+            except ValueError:
+                continue
+            for name, b in REASONS.items():
+                if bits & b:
+                    reasons.add(name)
+        try:
+            os.remove(self.path)
+        except OSError:
+            pass
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        top = max(sm)
+        loaded = [v for v in sm if v >= 0.5 * top] or sm
+        return {"sm_mhz": statistics.median(loaded), "sm_max_mhz": max(mx),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup(args):
+    import torch
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    if torch.cuda.is_available():
+        torch.cuda.set_device(local)
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(ws, v):
+    if ws == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def make_problem(cfg_name, device):
+    from emc_gb300 import synthetic as S
+    return S.make_problem(S.CONFIGS[cfg_name], device=device)
+
+
+def workload_desc(prob, precision, insert):
+    c = prob.cfg
+    return {"workload": f"{c.name}: {c.side}^3 model, {c.n_images} patterns {c.side}x{c.side} "
+                        f"(~{c.photons:g} photons, scale U{c.scale}, beamstop {c.beamstop} px), "
+                        f"{prob.quats.shape[0]} rotations (n={c.rot_n}), one full EMC iteration",
+            "side": c.side, "n_images": c.n_images, "n_rot": int(prob.quats.shape[0]),
+            "p_eff": int(prob.mask.sum()), "diff": "poisson (reference)", "interp": "nearest",
+            "precision": precision, "insert": insert,
+            "l2": "inputs larger than L2 (patterns 1.3 GB, responsibilities 2 GB per step)"}
+
+
+# ---------------------------------------------------- CPU (oracle) leg ----
+def cpu_leg(prob, seconds):
+    """Times the oracle's restatement of the reference path (scaling,
+    likelihood, LSE, M-step, insertion, divide, normalise) on a sample of
+    rotations x patterns of the workload, full detector.  Returns pairs/s."""
+    import numpy as np
+    from oracle import oracle as O
+    s = prob.cfg.side
+    cores = os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(cores))
+
+    def run(nr, ni):
+        t0 = time.perf_counter()
+        O.ref_iteration(prob.init_model, prob.images[:ni], prob.mask, prob.x, prob.y, prob.z,
+                        prob.quats[:nr], prob.weights[:nr], O.sigma_at(0), s)
+        return time.perf_counter() - t0
+
+    nr, ni = 8, 64
+    t = run(nr, ni)
+    scale = max(1.0, seconds / max(t, 1e-3))
+    ni2 = int(min(prob.images.shape[0], ni * max(1.0, scale ** 0.5)))
+    nr2 = int(min(prob.quats.shape[0], nr * max(1.0, scale / (ni2 / ni))))
+    t2 = run(nr2, ni2)
+    return dict(value=nr2 * ni2 / t2, unit=UNIT, cores=cores, kind="port",
+                sample=f"{nr2} rotations x {ni2} patterns of the {prob.cfg.name} workload, "
+                       f"full {s}x{s} detector, one reference-semantics iteration "
+                       f"(oracle/emc_oracle.c, OpenMP), {t2:.1f} s"), t2
+
+
+# ------------------------------------------------------------ GPU leg ----
+def run_ours(args):
+    import numpy as np
+    import torch
+
+    import emc_gb300 as E
+
+    ws, rank, local = dist_setup(args)
+    dev = torch.device(f"cuda:{local}")
+    prob = make_problem(args.config, "cuda")
+    s, R, N = prob.cfg.side, prob.quats.shape[0], prob.images.shape[0]
+    ctx = E.Context(local)
+    # one explicit stream for torch copies and library kernels (the legacy
+    # default stream has handle 0, which the library maps to its own stream)
+    torch_stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(torch_stream)
+    ctx.set_stream(torch_stream.cuda_stream)
+    T = lambda a, dt=torch.float32: torch.as_tensor(np.ascontiguousarray(a), dtype=dt, device=dev)
+    images, mask = T(prob.images), T(prob.mask, torch.int32)
+    x, y, z, rot, w = T(prob.x), T(prob.y), T(prob.z), T(prob.quats), T(prob.weights)
+    insert = E.INSERT_DETERMINISTIC if args.insert == "deterministic" else E.INSERT_ATOMIC
+
+    def new_plan(prec):
+        p = E.Plan(ctx, s, N, R, precision=prec, insert_mode=insert)
+        p.bind(images, mask, x, y, z, rot, w)
+        return p
+
+    precision = args.precision
+    plan = None
+    if precision in ("auto", "mixed"):
+        try:
+            plan = new_plan(E.PREC_MIXED)
+            precision = "mixed"
+        except E.EmcError:
+            if args.precision == "mixed":
+                raise
+            plan = None
+    if plan is None:
+        plan = new_plan(E.PREC_FP32)
+        precision = "fp32"
+    plan.set_profiling(True)
+    model = T(prob.init_model)
+    weight = torch.empty_like(model)
+    sig = [E.sigma_schedule(i, 0.4, 0.12, 25) for i in range(args.warmup + args.steps)]
+    for i in range(args.warmup):
+        plan.iterate(model, weight, sig[i], stats=False)
+    torch.cuda.synchronize()
+
+    # ---- timed region
+    sampler = ClockSampler(local)
+    sampler.start()
+    launches0 = ctx.kernel_launches
+    barrier(ws)
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(torch_stream)
+    estep_ms = []
+    phases = []
+    for k in range(args.steps):
+        plan.iterate(model, weight, sig[args.warmup + k], stats=False)
+        ph = plan.phase_ms()
+        phases.append(ph)
+        estep_ms.append(ph["estep"])
+    ev1.record(torch_stream)
+    torch.cuda.synchronize()
+    barrier(ws)
+    launches = ctx.kernel_launches - launches0
+    clocks = sampler.stop()
+    ms_total = ev0.elapsed_time(ev1)
+    ms_step = max_over_ranks(ws, ms_total / args.steps)
+    pairs = float(R) * N
+    value = pairs * ws / (ms_step / 1e3)
+    st = plan.iterate(model, weight, sig[-1])
+
+    # ---- plain FP32 path on the same GPU (the x10 denominator)
+    plain = None
+    if precision == "mixed" and args.plain_steps > 0:
+        pplan = new_plan(E.PREC_FP32)
+        m2 = T(prob.init_model)
+        w2 = torch.empty_like(m2)
+        pplan.iterate(m2, w2, sig[0], stats=False)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(torch_stream)
+        for k in range(args.plain_steps):
+            pplan.iterate(m2, w2, sig[k], stats=False)
+        e1.record(torch_stream)
+        torch.cuda.synchronize()
+        pms = e0.elapsed_time(e1) / args.plain_steps
+        plain = {"ms_per_step": pms, "pairs_per_s": pairs / (pms / 1e3),
+                 "iter_per_s": 1e3 / pms}
+        pplan.close()
+    elif precision == "fp32":
+        plain = {"ms_per_step": ms_step, "pairs_per_s": pairs / (ms_step / 1e3),
+                 "iter_per_s": 1e3 / ms_step, "note": "the measured path is the plain FP32 path"}
+
+    # ---- end to end through the public API with host buffers
+    h_images = torch.from_numpy(prob.images).pin_memory()
+    h_model = torch.from_numpy(prob.init_model).pin_memory()
+    h_out_m = torch.empty_like(h_model).pin_memory()
+    h_out_w = torch.empty_like(h_model).pin_memory()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(torch_stream)
+    lls = []
+    for k in range(args.e2e_steps):
+        images.copy_(h_images, non_blocking=True)
+        model.copy_(h_model, non_blocking=True)
+        plan.bind(images, mask, x, y, z, rot, w)
+        stk = plan.iterate(model, weight, sig[k])
+        h_out_m.copy_(model, non_blocking=True)
+        h_out_w.copy_(weight, non_blocking=True)
+        lls.append(stk.total_loglik)
+    e1.record(torch_stream)
+    torch.cuda.synchronize()
+    wall = (time.perf_counter() - t0) / args.e2e_steps
+    e2e_ms = max(e0.elapsed_time(e1) / args.e2e_steps, wall * 1e3)
+    e2e_ms = max_over_ranks(ws, e2e_ms)
+    e2e = {"value": pairs * ws / (e2e_ms / 1e3), "unit": UNIT,
+           "h2d_bytes_per_step": int(prob.images.nbytes + prob.init_model.nbytes),
+           "d2h_bytes_per_step": int(2 * prob.init_model.nbytes + 8 * 4),
+           "ms_per_step": e2e_ms}
+
+    # ---- roofline of the dominant kernel (E-step)
+    peaks = load_peaks()
+    p_eff = int(prob.mask.sum())
+    flops = 8.0 * p_eff * pairs  # 4 GEMM-equivalents (num, den, B, C) x 2 FLOP
+    est = statistics.mean(estep_ms)
+    achieved = flops / (est / 1e3) / 1e12
+    kernel = "estep_tc" if precision == "mixed" else "estep_fp32"
+    traffic = profile_traffic(kernel)
+    roofline = {"bound": "tensor", "kernel": kernel, "achieved": achieved,
+                "peak": peaks["bf16"], "unit": "TFLOP/s", "frac": achieved / peaks["bf16"],
+                "peak_source": f"bf16_tflops of {peaks['source']} peaks",
+                "flops_per_launch": flops, "ms_per_launch": est,
+                "traffic": traffic}
+    if precision == "fp32":
+        roofline["note"] = ("plain FP32 SIMT kernel; against the FP32 FMA pipe "
+                            "(152 SMs x 128 lanes x 2 x sm clock) it runs at "
+                            f"{achieved / (152 * 128 * 2 * (clocks.get('sm_mhz') or 1900) * 1e6 / 1e12):.2f}")
+    phase_mean = {k: statistics.mean(p[k] for p in phases) for k in phases[0]}
+
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        cpu, _ = cpu_leg(prob, args.cpu_seconds)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32" if precision == "fp32" else "f16/f32",
+            "data": "synthetic (seeded; shapes of the mid-size configuration)",
+            "config": workload_desc(prob, precision, args.insert),
+            "iter_per_s": ws * 1e3 / ms_step,
+            "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "plain_fp32": plain,
+            "speedup_vs_plain_fp32": (plain["ms_per_step"] / ms_step) if plain else None,
+            "phase_ms": phase_mean, "gpu_launches": launches, "clocks": clocks,
+            "total_loglik": st.total_loglik, "captured_mass": st.captured_mass,
+            "workspace_gb": plan.workspace_bytes / 1e9,
+        }
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def run_reference(args):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from emc_gb300 import synthetic as S
+    try:
+        import torch
+        dev = "cuda" if torch.cuda.is_available() else None
+    except Exception:
+        dev = None
+    prob = S.make_problem(S.CONFIGS[args.config], device=dev)
+    vals = []
+    info = None
+    for k in range(args.warmup + args.steps):
+        info, secs = cpu_leg(prob, max(2.0, args.cpu_seconds / max(1, args.steps)))
+        if k >= args.warmup:
+            vals.append(info["value"])
+    v = statistics.mean(vals)
+    R, N = prob.quats.shape[0], prob.images.shape[0]
+    line = {"metric": METRIC, "impl": "reference", "value": v, "unit": UNIT, "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": R * N / v * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32/f64",
+            "data": "synthetic (seeded; shapes of the mid-size configuration)",
+            "config": workload_desc(prob, "reference (quirk-exact CPU restatement)", "sequential"),
+            "cpu_baseline": {**info, "value": v},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -260,6 +260,18 @@ class Plan:
                                               C.byref(st) if stats else None), "iterate")
         return st if stats else None
 
+    PHASES = ("expand", "estep", "lse", "mprep", "mstep", "finish")
+
+    def set_profiling(self, on: bool = True):
+        self.ctx._check(self._lib.emc_plan_set_profiling(self._h, int(on)), "plan_set_profiling")
+
+    def phase_ms(self) -> dict:
+        """Per-phase durations (ms) of the last iteration, from CUDA events
+        recorded on the context stream."""
+        out = (C.c_float * 6)()
+        self.ctx._check(self._lib.emc_plan_phase_ms(self._h, out, 6), "plan_phase_ms")
+        return dict(zip(self.PHASES, [float(v) for v in out]))
+
     def results(self):
         r, s, l = C.c_void_p(), C.c_void_p(), C.c_void_p()
         self.ctx._check(self._lib.emc_plan_results(self._h, C.byref(r), C.byref(s), C.byref(l)),

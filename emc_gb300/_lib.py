@@ -85,6 +85,8 @@ SIGNATURES: dict[str, tuple] = {
     "emc_plan_bind": (I, [P, P, P, P, P, P, P, P]),
     "emc_iterate": (I, [P, P, P, F, C.POINTER(IterStats)]),
     "emc_plan_results": (I, [P, C.POINTER(P), C.POINTER(P), C.POINTER(P)]),
+    "emc_plan_set_profiling": (I, [P, I]),
+    "emc_plan_phase_ms": (I, [P, P, I]),
 }
 
 _lib = None

@@ -471,7 +471,7 @@ __global__ void __launch_bounds__(TPB, 1) estep_pois_fp32_kernel(EstepArgs a) {
   ld_tile(a.S, a.Kp, r0, a.R, 0, vr);
   ld_tile(a.Kraw, a.Kp, n0, a.N, 0, vk);
   for (int kb = 0; kb < nk; ++kb) {
-    st_tile_t(s0, vr, [](float s) { return __logf(fmaxf(s, kSliceFloor)); });
+    st_tile_t(s0, vr, [](float s) { return logf(fmaxf(s, kSliceFloor)); });
     st_tile_t(s2, vk, [](float v) { return v; });
     __syncthreads();
     if (kb + 1 < nk) {
@@ -611,16 +611,22 @@ struct InsertCtx {
   float* weight;
   unsigned long long* fix_m;
   unsigned long long* fix_w;
-  double scale_m, scale_w;  // fixed-point scales (deterministic mode)
+  const double* bounds;  // {model, weight} inserted-mass bounds (deterministic mode)
   int side;
   int interp;
   int deterministic;
 };
 
+// Fixed-point scale of the deterministic insertion: 2^61 / bound, so no
+// partial sum can leave the signed 64-bit range.
+__host__ __device__ inline double fixed_scale(double bound) {
+  return bound > 0.0 ? 2305843009213693952.0 / bound : 1.0;
+}
+
 __device__ __forceinline__ void add_voxel(const InsertCtx& c, size_t v, float val, float w) {
   if (c.deterministic) {
-    atomicAdd(c.fix_m + v, (unsigned long long)__double2ll_rn((double)val * c.scale_m));
-    atomicAdd(c.fix_w + v, (unsigned long long)__double2ll_rn((double)w * c.scale_w));
+    atomicAdd(c.fix_m + v, (unsigned long long)__double2ll_rn((double)val * fixed_scale(c.bounds[0])));
+    atomicAdd(c.fix_w + v, (unsigned long long)__double2ll_rn((double)w * fixed_scale(c.bounds[1])));
   } else {
     atomicAdd(c.model + v, val);
     atomicAdd(c.weight + v, w);
@@ -750,10 +756,39 @@ __global__ void __launch_bounds__(TPB, 1) mstep_fp32_kernel(MstepArgs a) {
 }
 
 // ------------------------------------------------------- finishing -------
+// Upper bounds of the inserted model and weight mass (deterministic mode):
+// 1.25 * sum_r sum_i Q_ri K_i and 1.25 * P_eff * sum_r T_r, FP64, fixed order.
+__global__ void insert_bounds_kernel(const double* __restrict__ row_mass,
+                                     const double* __restrict__ row_bound, int R, int P_eff,
+                                     double* __restrict__ out) {
+  __shared__ double sm[256], sw[256];
+  double m = 0.0, w = 0.0;
+  for (int r = threadIdx.x; r < R; r += blockDim.x) {
+    m += row_bound[r];
+    w += row_mass[r];
+  }
+  sm[threadIdx.x] = m;
+  sw[threadIdx.x] = w;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) {
+      sm[threadIdx.x] += sm[threadIdx.x + o];
+      sw[threadIdx.x] += sw[threadIdx.x + o];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    out[0] = 1.25 * sm[0] + 1e-30;
+    out[1] = 1.25 * sw[0] * (double)P_eff + 1e-30;
+  }
+}
+
 __global__ void fixed_to_model_kernel(const unsigned long long* __restrict__ fm,
-                                      const unsigned long long* __restrict__ fw, double inv_m,
-                                      double inv_w, float* __restrict__ model,
+                                      const unsigned long long* __restrict__ fw,
+                                      const double* __restrict__ bounds, float* __restrict__ model,
                                       float* __restrict__ weight, long long n) {
+  const double inv_m = 1.0 / fixed_scale(bounds[0]);
+  const double inv_w = 1.0 / fixed_scale(bounds[1]);
   const long long stride = (long long)gridDim.x * blockDim.x;
   for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += stride) {
     model[v] = (float)((double)(long long)fm[v] * inv_m);
@@ -822,6 +857,9 @@ extern "C" int emc_plan_create(emc_ctx* ctx, const emc_plan_desc* desc, emc_plan
 extern "C" int emc_plan_destroy(emc_plan* p) {
   if (!p) return EMC_OK;
   if (p->ctx) cudaStreamSynchronize(p->ctx->stream);
+  for (auto& e : p->ev)
+    if (e) cudaEventDestroy(e);
+  if (p->tc) tc_free(p);
   for (void* a : p->allocs) cudaFree(a);
   delete p;
   return EMC_OK;
@@ -836,8 +874,8 @@ extern "C" int emc_plan_bind(emc_plan* p, const float* d_images, const int* d_ma
   emc_ctx* ctx = p->ctx;
   EMC_REQUIRE(ctx, d_images && d_mask && d_x && d_y && d_z && d_rot && d_rot_weights,
               "plan_bind: null pointer");
-  EMC_REQUIRE(ctx, !p->bound, "plan_bind: plan already bound");
   const int n2 = p->n2, N = p->d.n_images;
+  const int prev_P = p->P_eff;
   // Mask -> compacted pixel list (host; once per plan).
   std::vector<int> hmask(n2);
   EMC_CUDA(ctx, cudaMemcpyAsync(hmask.data(), d_mask, sizeof(int) * n2, cudaMemcpyDeviceToHost,
@@ -849,10 +887,15 @@ extern "C" int emc_plan_bind(emc_plan* p, const float* d_images, const int* d_ma
     if (hmask[q]) pix.push_back(q);
   }
   EMC_REQUIRE(ctx, !pix.empty(), "plan_bind: mask is empty");
+  EMC_REQUIRE(ctx, prev_P == 0 || prev_P == (int)pix.size(),
+              "plan_bind: a re-bind must keep the mask's pixel count (%d != %d)", (int)pix.size(),
+              prev_P);
+  p->bound = false;
   p->P_eff = (int)pix.size();
   p->Kp = ceil_div(p->P_eff, 128) * 128;  // whole 128-pixel M-step tiles
   pix.resize(p->Kp, -1);
   int rc = EMC_OK;
+  if (prev_P == 0) {
   if (!rc) rc = alloc_n(p, &p->pix, p->Kp);
   if (!rc) rc = alloc_n(p, &p->cx, p->Kp);
   if (!rc) rc = alloc_n(p, &p->cy, p->Kp);
@@ -862,6 +905,7 @@ extern "C" int emc_plan_bind(emc_plan* p, const float* d_images, const int* d_ma
   if (!rc && p->d.precision == EMC_PREC_FP32) {
     rc = alloc_n(p, &p->Kt, (size_t)N * p->Kp);
     if (!rc) rc = alloc_n(p, &p->K2, (size_t)N * p->Kp);
+  }
   }
   if (rc) return rc;
   EMC_CUDA(ctx, cudaMemcpyAsync(p->pix, pix.data(), sizeof(int) * p->Kp, cudaMemcpyHostToDevice,
@@ -940,44 +984,19 @@ static int plan_estep_fp32(emc_plan* p, float sigma) {
   return after_launch(ctx, "estep_fp32_kernel");
 }
 
-static InsertCtx make_insert_ctx(emc_plan* p, float* model, float* weight, double bm, double bw) {
+static InsertCtx make_insert_ctx(emc_plan* p, float* model, float* weight) {
   InsertCtx c;
   c.model = model;
   c.weight = weight;
   c.fix_m = p->fix_m;
   c.fix_w = p->fix_w;
+  c.bounds = p->red + kRedBoundM;
   c.side = p->d.side;
   c.interp = p->d.interp;
   c.deterministic = p->d.insert_mode == EMC_INSERT_DETERMINISTIC;
-  // 2^61 / bound: no partial sum can exceed 2^61 < 2^63.
-  c.scale_m = bm > 0 ? std::ldexp(1.0, 61) / bm : 1.0;
-  c.scale_w = bw > 0 ? std::ldexp(1.0, 61) / bw : 1.0;
   return c;
 }
 
-namespace emc {
-// Inserted-mass bounds of the deterministic mode (host, after mprep).
-int plan_insert_bounds(emc_plan* p, double* bm, double* bw) {
-  emc_ctx* ctx = p->ctx;
-  const int R = p->d.n_rot;
-  std::vector<double> h(2 * (size_t)R);
-  double* row_mass = p->red + kRedSlots;
-  double* row_bound = row_mass + p->Rp;
-  EMC_CUDA(ctx, cudaMemcpyAsync(h.data(), row_mass, sizeof(double) * R, cudaMemcpyDeviceToHost,
-                                ctx->stream));
-  EMC_CUDA(ctx, cudaMemcpyAsync(h.data() + R, row_bound, sizeof(double) * R,
-                                cudaMemcpyDeviceToHost, ctx->stream));
-  EMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-  double m = 0.0, w = 0.0;
-  for (int r = 0; r < R; ++r) {
-    m += h[R + r];
-    w += h[r];
-  }
-  *bm = 1.25 * m + 1e-30;
-  *bw = 1.25 * w * (double)p->P_eff + 1e-30;
-  return EMC_OK;
-}
-}  // namespace emc
 
 static int plan_mstep_fp32(emc_plan* p, float* model, float* weight, const InsertCtx& ins) {
   emc_ctx* ctx = p->ctx;
@@ -1012,38 +1031,48 @@ extern "C" int emc_iterate(emc_plan* p, float* d_model, float* d_weight, float s
   const int R = p->d.n_rot, N = p->d.n_images;
   const long long n3 = (long long)p->d.side * p->d.side * p->d.side;
   int rc;
+  auto mark = [&](int i) -> int {
+    if (p->profiling) EMC_CUDA(ctx, cudaEventRecord(p->ev[i], ctx->stream));
+    return EMC_OK;
+  };
+  if ((rc = mark(0))) return rc;
   EMC_CUDA(ctx, cudaMemsetAsync(p->flags + 4, 0, sizeof(int), ctx->stream));
   // expand
   if ((rc = plan_expand(p, d_model))) return rc;
+  if ((rc = mark(1))) return rc;
   // scaling + likelihood + per-tile LSE partials
   if (p->d.precision == EMC_PREC_MIXED)
     rc = tc_estep(p, sigma);
   else
     rc = plan_estep_fp32(p, sigma);
   if (rc) return rc;
+  if ((rc = mark(2))) return rc;
   // normaliser
   lse_combine_kernel<<<ceil_div(N, 256), 256, 0, ctx->stream>>>(p->part, p->n_rt, N, p->lse);
   if ((rc = after_launch(ctx, "lse_combine_kernel"))) return rc;
   finite_sum_kernel<<<1, 256, 0, ctx->stream>>>(p->lse, N, p->red + kRedLL);
   if ((rc = after_launch(ctx, "finite_sum_kernel"))) return rc;
+  if ((rc = mark(3))) return rc;
   double* row_mass = p->red + kRedSlots;
   double* row_bound = row_mass + p->Rp;
   mprep_kernel<<<R, 256, 0, ctx->stream>>>(p->L, p->PHI, p->lse, p->Ksum, R, N,
                                             p->d.precision == EMC_PREC_FP32 ? p->Q : nullptr,
                                             p->Np, p->T, row_mass, row_bound);
   if ((rc = after_launch(ctx, "mprep_kernel"))) return rc;
+  if ((rc = mark(4))) return rc;
   // M-step into zeroed accumulators
-  double bm = 0.0, bw = 0.0;
   const bool det = p->d.insert_mode == EMC_INSERT_DETERMINISTIC;
   if (det) {
-    if ((rc = plan_insert_bounds(p, &bm, &bw))) return rc;
+    insert_bounds_kernel<<<1, 256, 0, ctx->stream>>>(row_mass, row_bound, R, p->P_eff,
+                                                      p->red + kRedBoundM);
+    if ((rc = after_launch(ctx, "insert_bounds_kernel"))) return rc;
     EMC_CUDA(ctx, cudaMemsetAsync(p->fix_m, 0, sizeof(unsigned long long) * n3, ctx->stream));
     EMC_CUDA(ctx, cudaMemsetAsync(p->fix_w, 0, sizeof(unsigned long long) * n3, ctx->stream));
   } else {
     EMC_CUDA(ctx, cudaMemsetAsync(d_model, 0, sizeof(float) * n3, ctx->stream));
     EMC_CUDA(ctx, cudaMemsetAsync(d_weight, 0, sizeof(float) * n3, ctx->stream));
   }
-  InsertCtx ins = make_insert_ctx(p, d_model, d_weight, bm, bw);
+  InsertCtx ins = make_insert_ctx(p, d_model, d_weight);
   if (p->d.precision == EMC_PREC_MIXED)
     rc = tc_mstep(p, d_model, d_weight);
   else
@@ -1051,10 +1080,11 @@ extern "C" int emc_iterate(emc_plan* p, float* d_model, float* d_weight, float s
   if (rc) return rc;
   if (det) {
     const int nb = (int)std::min<long long>(ceil_div(n3, 256), (long long)ctx->sm_count * 8);
-    fixed_to_model_kernel<<<nb, 256, 0, ctx->stream>>>(p->fix_m, p->fix_w, 1.0 / ins.scale_m,
-                                                        1.0 / ins.scale_w, d_model, d_weight, n3);
+    fixed_to_model_kernel<<<nb, 256, 0, ctx->stream>>>(p->fix_m, p->fix_w, ins.bounds, d_model,
+                                                        d_weight, n3);
     if ((rc = after_launch(ctx, "fixed_to_model_kernel"))) return rc;
   }
+  if ((rc = mark(5))) return rc;
   // divide, normalise, blur
   if ((rc = launch_divide_by_weight(ctx, d_model, d_weight, n3))) return rc;
   double* mean_stats = p->red + kRedMean;
@@ -1068,6 +1098,7 @@ extern "C" int emc_iterate(emc_plan* p, float* d_model, float* d_weight, float s
   if (p->d.blur_sigma > 0.0f) {
     if ((rc = launch_blur(ctx, d_model, p->d.side, p->d.blur_sigma))) return rc;
   }
+  if ((rc = mark(6))) return rc;
   if (stats) {
     double h[kRedSlots];
     int bad = 0;
@@ -1086,6 +1117,26 @@ extern "C" int emc_iterate(emc_plan* p, float* d_model, float* d_weight, float s
     stats->bad_pairs = bad;
     stats->reserved = 0;
   }
+  return EMC_OK;
+}
+
+extern "C" int emc_plan_set_profiling(emc_plan* p, int on) {
+  if (!p) return EMC_ERR_INVALID;
+  emc_ctx* ctx = p->ctx;
+  if (on && !p->ev[0]) {
+    for (auto& e : p->ev) EMC_CUDA(ctx, cudaEventCreate(&e));
+  }
+  p->profiling = on != 0;
+  return EMC_OK;
+}
+
+extern "C" int emc_plan_phase_ms(emc_plan* p, float* ms, int n) {
+  if (!p || !ms || n < 0) return EMC_ERR_INVALID;
+  emc_ctx* ctx = p->ctx;
+  EMC_REQUIRE(ctx, p->profiling, "plan_phase_ms: profiling is off");
+  EMC_CUDA(ctx, cudaEventSynchronize(p->ev[emc_plan::kPhases]));
+  for (int i = 0; i < n && i < emc_plan::kPhases; ++i)
+    EMC_CUDA(ctx, cudaEventElapsedTime(ms + i, p->ev[i], p->ev[i + 1]));
   return EMC_OK;
 }
 

@@ -225,7 +225,7 @@ static BlurTaps blur_taps(int side, double sigma, std::vector<float>& g) {
   for (int n = 0; n < side; ++n) g[n] = (float)gd[n];
   int h = 0;
   const double tol = 1e-9 * std::fabs(gd[0]);
-  for (int n = 1; n < (side + 1) / 2; ++n)
+  for (int n = 1; n <= side / 2; ++n)  // offset side/2 is its own mirror for even sides
     if (std::fabs(gd[n]) > tol) h = n;
   BlurTaps t;
   if (2 * h + 1 >= side) {  // the whole circle: offsets -(side-1)/2 .. side/2

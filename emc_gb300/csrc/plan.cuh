@@ -52,7 +52,6 @@ struct emc_plan {
   float* rot_cnt = nullptr; // [Rp] count_r (pixels with s > 0)
   float* rot_A = nullptr;   // [Rp] sum s^2/(s+c) over s > 0
   float* rot_ssum = nullptr;// [Rp] sum max(s, floor) (true Poisson)
-  __half* Gop = nullptr;    // [6][Rp][Kp] rotation operands (tensor-core path)
 
   // responsibilities
   float* L = nullptr;      // [R][N] log-likelihood, then normalised responsibility
@@ -67,6 +66,13 @@ struct emc_plan {
   unsigned long long* fix_m = nullptr;  // [s^3] fixed-point model (deterministic insert)
   unsigned long long* fix_w = nullptr;
   int* flags = nullptr;    // device status words
+
+  // per-phase CUDA events on the context stream (emc_plan_set_profiling)
+  static constexpr int kPhases = 6;  // expand, estep, lse, mprep, mstep, finish
+  bool profiling = false;
+  cudaEvent_t ev[kPhases + 1] = {};
+
+  void* tc = nullptr;  // tensor-core state (tensor maps, rotation operands)
 
   std::vector<void*> allocs;
   size_t bytes = 0;
@@ -91,5 +97,6 @@ int plan_alloc(emc_plan* p, void** ptr, size_t bytes);
 int tc_bind(emc_plan* p);
 int tc_estep(emc_plan* p, float sigma);
 int tc_mstep(emc_plan* p, float* model, float* weight);
+void tc_free(emc_plan* p);
 
 }  // namespace emc

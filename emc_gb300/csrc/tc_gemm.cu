@@ -1,8 +1,749 @@
-// Tensor-core (tcgen05) E-step and M-step of the fused iteration.
+// Tensor-core (tcgen05 + TMA) E-step and M-step of the fused iteration.
+//
+// E-step.  For a tile of 128 patterns (M, one TMEM lane each) x 128
+// rotations (N) the reference's "poisson" likelihood with per-pair scaling
+// (emc_cuda.cu:196-216, 438-454) is expanded into four contractions over the
+// compacted pixels, accumulated in TMEM (FP32, 4 x 128 columns = all 512):
+//   num = sum k^2 [s > 1e-10]             (K^2 hi + lo)  x  M'         exact
+//   den = sum k s [s > 1e-10]             K              x  (M' S) hi
+//   B   = sum k s/(s+c) [s > 0]           K              x  (G hi + lo)
+//   C   = sum k^2 /(s+c) [s > 0]          (K^2 hi + lo)  x  (H hi + lo)
+// so that with 1/phi = den/num:  S_ri = A_r - 2 B/phi + C/phi^2  and
+// L_ri = log w_r - S_ri / (2 count_r sigma^2).  Counts are integers <= 2048,
+// exact in FP16; K^2 * 2^-7 is split exactly into two FP16 terms; the
+// rotation-side factors are split hi + lo (the lo x lo products are dropped,
+// relative size 2^-22).  The epilogue (4 warps, one pattern row per thread)
+// forms L and phi, stores them coalesced along patterns, and keeps a running
+// (max, sum exp) per pattern over the tile's rotations: the per-tile LSE
+// partials that the FP64 normaliser combines.
+//
+// M-step.  U = Q K^T over the patterns for a tile of 128 rotations x 256
+// pixels, Q = P / phi split hi + lo in FP16 with a per-rotation power-of-two
+// scale, K the exact FP16 counts; the epilogue inserts T_r * (U / T_r) at
+// the rotated pixel (nearest or trilinear) with weight T_r -- the slice never
+// reaches HBM (emc_atomic.cu:88-132, 183-200).
+//
+// Pipeline: warp 0 issues TMA loads into a ring of shared-memory stages
+// (mbarrier full/empty handshake), warp 1 owns TMEM and issues tcgen05.mma
+// from one lane, warps 2-5 run the epilogue.  Every wait is bounded and
+// reports through a device status word (EMC_ERR_TIMEOUT on the host).
+#include <cuda.h>
+#include <cuda_fp16.h>
+
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "geometry.cuh"
 #include "plan.cuh"
+#include "ptx.cuh"
 
 namespace emc {
-int tc_bind(emc_plan* p) { return fail(p->ctx, EMC_ERR_UNSUPPORTED, "mixed precision path not built yet"); }
-int tc_estep(emc_plan* p, float) { return fail(p->ctx, EMC_ERR_UNSUPPORTED, "mixed precision path not built yet"); }
-int tc_mstep(emc_plan* p, float*, float*) { return fail(p->ctx, EMC_ERR_UNSUPPORTED, "mixed precision path not built yet"); }
+
+// ------------------------------------------------------- tensor maps -----
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                  const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                  const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_fn() {
+  static EncodeTiledFn fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPoint("cuTensorMapEncodeTiled", &p, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (EncodeTiledFn)p;
+  }
+  return fn;
+}
+
+// Row-major FP16 matrix [rows][cols] (cols contiguous), tiles of
+// box_rows x box_cols, 64B or 128B swizzle (box_cols * 2 == swizzle span).
+static int make_map(emc_ctx* ctx, CUtensorMap* map, const void* base, uint64_t rows,
+                    uint64_t cols, uint32_t box_rows, uint32_t box_cols) {
+  EncodeTiledFn fn = encode_fn();
+  if (!fn) return fail(ctx, EMC_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
+  if (((uintptr_t)base & 15) || ((cols * 2) & 15))
+    return fail(ctx, EMC_ERR_INTERNAL, "tensor map: misaligned base or pitch");
+  cuuint64_t dims[2] = {cols, rows};
+  cuuint64_t strides[1] = {cols * 2};
+  cuuint32_t box[2] = {box_cols, box_rows};
+  cuuint32_t estr[2] = {1, 1};
+  const CUtensorMapSwizzle sw =
+      box_cols * 2 == 128 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B;
+  CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, const_cast<void*>(base), dims, strides,
+                  box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, sw, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return fail(ctx, EMC_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+  return EMC_OK;
+}
+
+// ---------------------------------------------------- pattern operands ---
+constexpr float kK2Scale = 1.0f / 128.0f;  // K^2 * 2^-7 <= 2^15 for counts <= 2048
+constexpr float kMSScale = 1.0f / 256.0f;  // (M' S) * 2^-8 keeps slices below 2^24 in range
+
+// Counts -> FP16 operands, rows of Kp (patterns padded to Np with zeros):
+// Kh = k, K2h + K2l = k^2 * 2^-7 exactly.
+__global__ void tc_pattern_ops_kernel(const float* __restrict__ images, const int* __restrict__ pix,
+                                      int n2, int N, int Kp, __half* __restrict__ Kh,
+                                      __half* __restrict__ K2h, __half* __restrict__ K2l) {
+  const int i = blockIdx.y;
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= Kp) return;
+  float k = 0.0f;
+  if (i < N) {
+    const int p = pix[q];
+    if (p >= 0) k = __ldg(images + (size_t)i * n2 + p);
+  }
+  const float k2 = k * k * kK2Scale;  // exact: k^2 < 2^22
+  const __half hi = __float2half_rn(k2);
+  const __half lo = __float2half_rn(k2 - __half2float(hi));
+  const size_t o = (size_t)i * Kp + q;
+  Kh[o] = __float2half_rn(k);
+  K2h[o] = hi;
+  K2l[o] = lo;
+}
+
+// flags[pt][kb] = any K2l != 0 in rows pt*128..+127, cols kb*32..+31.
+__global__ void tc_k2lo_flags_kernel(const __half* __restrict__ K2l, int Kp,
+                                     unsigned char* __restrict__ flags, int nkb) {
+  const int pt = blockIdx.y, kb = blockIdx.x;
+  int any = 0;
+  for (int e = threadIdx.x; e < 128 * 32; e += blockDim.x) {
+    const int r = pt * 128 + e / 32, c = kb * 32 + e % 32;
+    if (__half2float(K2l[(size_t)r * Kp + c]) != 0.0f) any = 1;
+  }
+  any = __syncthreads_or(any);
+  if (threadIdx.x == 0) flags[(size_t)pt * nkb + kb] = (unsigned char)any;
+}
+
+// [rows][cols] -> [cols][rows], FP16, 32x32 tiles.
+__global__ void transpose_h_kernel(const __half* __restrict__ in, int rows, int cols,
+                                   __half* __restrict__ out) {
+  __shared__ __half t[32][33];
+  const int c0 = blockIdx.x * 32, r0 = blockIdx.y * 32;
+  for (int y = threadIdx.y; y < 32; y += blockDim.y) {
+    const int r = r0 + y, c = c0 + threadIdx.x;
+    t[y][threadIdx.x] = (r < rows && c < cols) ? in[(size_t)r * cols + c] : __float2half_rn(0.f);
+  }
+  __syncthreads();
+  for (int y = threadIdx.y; y < 32; y += blockDim.y) {
+    const int c = c0 + y, r = r0 + threadIdx.x;
+    if (c < cols && r < rows) out[(size_t)c * rows + r] = t[threadIdx.x][y];
+  }
+}
+
+// ---------------------------------------------------- rotation operands --
+constexpr float kPoisCf = 0.02f;
+
+// From the compacted slices S [Rp][Kp] (FP32): the six FP16 rotation-side
+// operands, each [Rp][Kp]: M' = [s > 1e-10], (M' s) 2^-8 hi, G = [s > 0]
+// s/(s+c) hi/lo, H = [s > 0] /(s+c) hi/lo.  flags[0] |= 4 when a slice value
+// does not fit the scaled FP16 range.
+__global__ void tc_rot_ops_kernel(const float* __restrict__ S, size_t n, __half* __restrict__ Mp,
+                                  __half* __restrict__ MSh, __half* __restrict__ Gh,
+                                  __half* __restrict__ Gl, __half* __restrict__ Hh,
+                                  __half* __restrict__ Hl, int* __restrict__ flags) {
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += stride) {
+    const float s = S[e];
+    const bool mp = (double)s > 1e-10;
+    const bool m = s > 0.0f;
+    const float ms = mp ? s * kMSScale : 0.0f;
+    if (ms > 60000.0f) atomicOr(flags, 4);
+    const float h = m ? 1.0f / (s + kPoisCf) : 0.0f;
+    const float g = m ? s * h : 0.0f;
+    const __half gh = __float2half_rn(g), hh = __float2half_rn(h);
+    Mp[e] = __float2half_rn(mp ? 1.0f : 0.0f);
+    MSh[e] = __float2half_rn(ms);
+    Gh[e] = gh;
+    Gl[e] = __float2half_rn(g - __half2float(gh));
+    Hh[e] = hh;
+    Hl[e] = __float2half_rn(h - __half2float(hh));
+  }
+}
+
+// ------------------------------------------------------------ E-step -----
+namespace es {
+constexpr int BM = 128;        // patterns per tile (TMEM lanes)
+constexpr int BN = 128;        // rotations per tile
+constexpr int BK = 32;         // pixels per stage (64 B rows, 64B swizzle)
+constexpr int STAGES = 3;
+constexpr int TILE_BYTES = 128 * BK * 2;  // 8 KB, both operand sides
+constexpr int NA = 3;          // K, K2h, K2l
+constexpr int NB = 6;          // M', MS, Gh, Gl, Hh, Hl
+constexpr int STAGE_BYTES = (NA + NB) * TILE_BYTES;
+constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 2048 + 1024;
+constexpr int THREADS = 192;
+constexpr int GROUP = 8;       // rotation tiles per raster group
+}  // namespace es
+
+struct TcEstepArgs {
+  int N, R, Kp, n_pt, n_rt, nkb;
+  const unsigned char* k2lo_any;  // [n_pt][nkb]
+  const float* rot_cnt;
+  const float* rot_A;
+  const float* rotw;
+  const float* cnorm;   // c_i (phi is stored as c_i num/den)
+  float inv2s2;         // 1 / (2 sigma^2)
+  int known_intensity;
+  float* L;
+  float* PHI;
+  float2* part;
+  int* bad;
+  int* status;
+};
+
+__global__ void __launch_bounds__(es::THREADS, 1)
+    tc_estep_kernel(const __grid_constant__ CUtensorMap mK, const __grid_constant__ CUtensorMap mK2h,
+                    const __grid_constant__ CUtensorMap mK2l, const __grid_constant__ CUtensorMap mMp,
+                    const __grid_constant__ CUtensorMap mMS, const __grid_constant__ CUtensorMap mGh,
+                    const __grid_constant__ CUtensorMap mGl, const __grid_constant__ CUtensorMap mHh,
+                    const __grid_constant__ CUtensorMap mHl, TcEstepArgs a) {
+  using namespace es;
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint64_t* full = (uint64_t*)(smem + STAGES * STAGE_BYTES);
+  uint64_t* empty = full + STAGES;
+  uint64_t* accum = empty + STAGES;
+  uint32_t* tmem_slot = (uint32_t*)(accum + 1);
+  float* s_A = (float*)(smem + STAGES * STAGE_BYTES + 256);
+  float* s_scale = s_A + BN;
+  float* s_lw = s_scale + BN;
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  // grouped raster: GROUP rotation tiles share each pattern tile in turn
+  const int t = blockIdx.x;
+  const int per_group = GROUP * a.n_pt;
+  const int g = t / per_group, within = t % per_group;
+  const int rt0 = g * GROUP;
+  const int gsz = min(GROUP, a.n_rt - rt0);
+  const int rt = rt0 + within % gsz;
+  const int pt = within / gsz;
+  const int n0 = pt * BM, r0 = rt * BN;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      ptx::mbar_init(&full[s], 1);
+      ptx::mbar_init(&empty[s], 1);
+    }
+    ptx::mbar_init(accum, 1);
+    ptx::fence_mbar_init();
+  }
+  if (threadIdx.x < BN) {
+    const int r = r0 + threadIdx.x;
+    const float cnt = r < a.R ? a.rot_cnt[r] : 0.0f;
+    s_A[threadIdx.x] = r < a.R ? a.rot_A[r] : 0.0f;
+    s_scale[threadIdx.x] = cnt > 0.0f ? a.inv2s2 / cnt : -1.0f;  // < 0: invalid rotation
+    s_lw[threadIdx.x] = r < a.R ? logf(a.rotw[r]) : 0.0f;
+  }
+  if (warp == 1) {
+    ptx::tmem_alloc(tmem_slot, 512);
+    ptx::tmem_relinquish();
+  }
+  ptx::tc_fence_before();
+  __syncthreads();
+  ptx::tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+  const unsigned char* flags = a.k2lo_any + (size_t)pt * a.nkb;
+
+  if (warp == 0) {
+    // ------------------------------------------------ TMA producer
+    if (lane == 0) {
+      const CUtensorMap* amap[NA] = {&mK, &mK2h, &mK2l};
+      const CUtensorMap* bmap[NB] = {&mMp, &mMS, &mGh, &mGl, &mHh, &mHl};
+      for (int kb = 0; kb < a.nkb; ++kb) {
+        const int s = kb % STAGES;
+        const uint32_t ph = (kb / STAGES) & 1;
+        if (!ptx::mbar_wait(&empty[s], ph ^ 1, a.status, 0)) break;
+        const bool lo = flags[kb] != 0;
+        ptx::mbar_arrive_expect_tx(&full[s], (NA + NB - (lo ? 0 : 1)) * TILE_BYTES);
+        unsigned char* st = smem + s * STAGE_BYTES;
+        for (int j = 0; j < NA; ++j) {
+          if (j == 2 && !lo) continue;
+          ptx::tma_load_2d(st + j * TILE_BYTES, amap[j], kb * BK, n0, &full[s]);
+        }
+        for (int j = 0; j < NB; ++j)
+          ptx::tma_load_2d(st + (NA + j) * TILE_BYTES, bmap[j], kb * BK, r0, &full[s]);
+      }
+    }
+  } else if (warp == 1) {
+    // ------------------------------------------------ MMA issuer
+    if (lane == 0) {
+      constexpr uint32_t idesc = ptx::idesc_f16(BM, BN);
+      bool ok = true;
+      for (int kb = 0; kb < a.nkb && ok; ++kb) {
+        const int s = kb % STAGES;
+        const uint32_t ph = (kb / STAGES) & 1;
+        if (!ptx::mbar_wait(&full[s], ph, a.status, 1)) {
+          ok = false;
+          break;
+        }
+        ptx::tc_fence_after();
+        const bool lo = flags[kb] != 0;
+        const uint32_t base = ptx::smem_u32(smem + s * STAGE_BYTES);
+#pragma unroll
+        for (int ks = 0; ks < BK / 16; ++ks) {
+          auto d = [&](int j) { return ptx::smem_desc(base + j * TILE_BYTES + ks * 32, 512, 4); };
+          const uint64_t aK = d(0), aK2h = d(1), aK2l = d(2);
+          const uint64_t bM = d(3), bMS = d(4), bGh = d(5), bGl = d(6), bHh = d(7), bHl = d(8);
+          const uint32_t acc = (kb | ks) ? 1u : 0u;
+          ptx::mma_f16(tmem + 0, aK2h, bM, idesc, acc);  // num
+          if (lo) ptx::mma_f16(tmem + 0, aK2l, bM, idesc, 1);
+          ptx::mma_f16(tmem + 128, aK, bMS, idesc, acc);  // den
+          ptx::mma_f16(tmem + 256, aK, bGh, idesc, acc);  // B
+          ptx::mma_f16(tmem + 256, aK, bGl, idesc, 1);
+          ptx::mma_f16(tmem + 384, aK2h, bHh, idesc, acc);  // C
+          ptx::mma_f16(tmem + 384, aK2h, bHl, idesc, 1);
+          if (lo) ptx::mma_f16(tmem + 384, aK2l, bHh, idesc, 1);
+        }
+        ptx::mma_commit(&empty[s]);
+      }
+      ptx::mma_commit(accum);  // fires when every MMA above has completed
+    }
+  } else {
+    // ------------------------------------------------ epilogue (warps 2-5)
+    const int quarter = warp & 3;  // TMEM lanes this warp may access
+    const int row = quarter * 32 + lane;
+    const int n = n0 + row;
+    const bool nok = n < a.N;
+    const float ci = nok ? a.cnorm[n] : 1.0f;
+    float m = -INFINITY, ssum = 0.0f;
+    int nbad = 0;
+    if (ptx::mbar_wait(accum, 0, a.status, 2)) {
+      ptx::tc_fence_after();
+      const uint32_t lane_addr = tmem + ((uint32_t)(quarter * 32) << 16);
+      for (int c0 = 0; c0 < BN; c0 += 16) {
+        float vn[16], vd[16], vb[16], vc[16];
+        ptx::tmem_ld16(lane_addr + 0 + c0, vn);
+        ptx::tmem_ld16(lane_addr + 128 + c0, vd);
+        ptx::tmem_ld16(lane_addr + 256 + c0, vb);
+        ptx::tmem_ld16(lane_addr + 384 + c0, vc);
+        ptx::tmem_wait_ld();
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          const int cl = c0 + j;
+          const int r = r0 + cl;
+          const float num = vn[j] * 128.0f, den = vd[j] * 256.0f;
+          const float B = vb[j], Cc = vc[j] * 128.0f;
+          const float sc = s_scale[cl];
+          bool ok = nok && r < a.R && sc > 0.0f;
+          float iphi = 1.0f, phi = 1.0f;
+          if (!a.known_intensity) {
+            ok = ok && num > 0.0f && den > 0.0f;
+            iphi = den / num;
+            phi = ci * num / den;
+          }
+          const float Sig = s_A[cl] - 2.0f * B * iphi + Cc * iphi * iphi;
+          const float L = ok ? s_lw[cl] - Sig * sc : -INFINITY;
+          if (nok && r < a.R) {
+            if (!ok) nbad++;
+            a.L[(size_t)r * a.N + n] = L;
+            a.PHI[(size_t)r * a.N + n] = ok ? phi : 1.0f;
+          }
+          if (L > m) {
+            ssum = ssum * expf(m - L) + 1.0f;
+            m = L;
+          } else if (L > -INFINITY) {
+            ssum += expf(L - m);
+          }
+        }
+      }
+    }
+    if (nok) a.part[(size_t)rt * a.N + n] = make_float2(m, ssum);
+    if (nbad) atomicAdd(a.bad, nbad);
+  }
+  ptx::tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    ptx::tc_fence_after();
+    ptx::tmem_dealloc(tmem, 512);
+  }
+}
+
+// ------------------------------------------------------------ M-step -----
+namespace ms {
+constexpr int BM = 128;   // rotations per tile (TMEM lanes)
+constexpr int BN = 256;   // pixels per tile
+constexpr int BK = 64;    // patterns per stage (128 B rows, 128B swizzle)
+constexpr int STAGES = 3;
+constexpr int A_BYTES = BM * BK * 2;  // 16 KB
+constexpr int B_BYTES = BN * BK * 2;  // 32 KB
+constexpr int STAGE_BYTES = 2 * A_BYTES + B_BYTES;
+constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 1024 + BM * (int)sizeof(RotMat);
+constexpr int THREADS = 192;
+constexpr int GROUP = 8;
+}  // namespace ms
+
+struct TcMstepArgs {
+  int R, Kp, Np, P_eff, n_qt, n_rt, nkb;
+  const float* T;
+  const float* qscale;  // [R] 2^-e_r
+  const float* rot;
+  const float *cx, *cy, *cz;
+  int side, interp, deterministic;
+  float* model;
+  float* weight;
+  unsigned long long* fix_m;
+  unsigned long long* fix_w;
+  const double* bounds;
+  int* status;
+};
+
+__device__ __forceinline__ double tc_fixed_scale(double b) {
+  return b > 0.0 ? 2305843009213693952.0 / b : 1.0;
+}
+
+__device__ __forceinline__ void tc_add(const TcMstepArgs& a, size_t v, float val, float w) {
+  if (a.deterministic) {
+    atomicAdd(a.fix_m + v, (unsigned long long)__double2ll_rn((double)val * tc_fixed_scale(a.bounds[0])));
+    atomicAdd(a.fix_w + v, (unsigned long long)__double2ll_rn((double)w * tc_fixed_scale(a.bounds[1])));
+  } else {
+    atomicAdd(a.model + v, val);
+    atomicAdd(a.weight + v, w);
+  }
+}
+
+__device__ __forceinline__ void tc_insert(const TcMstepArgs& a, const RotMat& R, float x, float y,
+                                          float z, float val, float w) {
+  const int side = a.side;
+  if (a.interp == EMC_INTERP_NEAREST) {
+    const long ix = lroundf(voxel_coord(side, rotate_row(R, 0, x, y, z)));
+    const long iy = lroundf(voxel_coord(side, rotate_row(R, 1, x, y, z)));
+    const long iz = lroundf(voxel_coord(side, rotate_row(R, 2, x, y, z)));
+    if (ix < 0 || ix >= side || iy < 0 || iy >= side || iz < 0 || iz >= side) return;
+    tc_add(a, ((size_t)iz * side + iy) * side + ix, val, w);
+  } else {
+    const float cx = voxel_coord(side, rotate_row(R, 0, x, y, z));
+    const float cy = voxel_coord(side, rotate_row(R, 1, x, y, z));
+    const float cz = voxel_coord(side, rotate_row(R, 2, x, y, z));
+    const float fx0 = floorf(cx), fy0 = floorf(cy), fz0 = floorf(cz);
+    const int x0 = (int)fx0, y0 = (int)fy0, z0 = (int)fz0;
+    const float tx = cx - fx0, ty = cy - fy0, tz = cz - fz0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      const int xi = x0 + (k & 1), yi = y0 + ((k >> 1) & 1), zi = z0 + (k >> 2);
+      if (xi < 0 || xi >= side || yi < 0 || yi >= side || zi < 0 || zi >= side) continue;
+      const float f = ((k & 1) ? tx : 1.0f - tx) * (((k >> 1) & 1) ? ty : 1.0f - ty) *
+                      ((k >> 2) ? tz : 1.0f - tz);
+      if (f <= 0.0f) continue;
+      tc_add(a, ((size_t)zi * side + yi) * side + xi, val * f, w * f);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(ms::THREADS, 1)
+    tc_mstep_kernel(const __grid_constant__ CUtensorMap mQh, const __grid_constant__ CUtensorMap mQl,
+                    const __grid_constant__ CUtensorMap mKt, TcMstepArgs a) {
+  using namespace ms;
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint64_t* full = (uint64_t*)(smem + STAGES * STAGE_BYTES);
+  uint64_t* empty = full + STAGES;
+  uint64_t* accum = empty + STAGES;
+  uint32_t* tmem_slot = (uint32_t*)(accum + 1);
+  RotMat* sR = (RotMat*)(smem + STAGES * STAGE_BYTES + 1024);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int t = blockIdx.x;
+  const int per_group = GROUP * a.n_qt;
+  const int g = t / per_group, within = t % per_group;
+  const int rt0 = g * GROUP;
+  const int gsz = min(GROUP, a.n_rt - rt0);
+  const int rt = rt0 + within % gsz;
+  const int qt = within / gsz;
+  const int r0 = rt * BM, q0 = qt * BN;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      ptx::mbar_init(&full[s], 1);
+      ptx::mbar_init(&empty[s], 1);
+    }
+    ptx::mbar_init(accum, 1);
+    ptx::fence_mbar_init();
+  }
+  if (threadIdx.x < BM) {
+    const int r = r0 + threadIdx.x;
+    if (r < a.R) sR[threadIdx.x] = quat_to_matrix(a.rot + 4 * (size_t)r);
+  }
+  if (warp == 1) {
+    ptx::tmem_alloc(tmem_slot, 256);
+    ptx::tmem_relinquish();
+  }
+  ptx::tc_fence_before();
+  __syncthreads();
+  ptx::tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      for (int kb = 0; kb < a.nkb; ++kb) {
+        const int s = kb % STAGES;
+        const uint32_t ph = (kb / STAGES) & 1;
+        if (!ptx::mbar_wait(&empty[s], ph ^ 1, a.status, 4)) break;
+        ptx::mbar_arrive_expect_tx(&full[s], STAGE_BYTES);
+        unsigned char* st = smem + s * STAGE_BYTES;
+        ptx::tma_load_2d(st, &mQh, kb * BK, r0, &full[s]);
+        ptx::tma_load_2d(st + A_BYTES, &mQl, kb * BK, r0, &full[s]);
+        ptx::tma_load_2d(st + 2 * A_BYTES, &mKt, kb * BK, q0, &full[s]);
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      constexpr uint32_t idesc = ptx::idesc_f16(BM, BN);
+      for (int kb = 0; kb < a.nkb; ++kb) {
+        const int s = kb % STAGES;
+        const uint32_t ph = (kb / STAGES) & 1;
+        if (!ptx::mbar_wait(&full[s], ph, a.status, 5)) break;
+        ptx::tc_fence_after();
+        const uint32_t base = ptx::smem_u32(smem + s * STAGE_BYTES);
+#pragma unroll
+        for (int ks = 0; ks < BK / 16; ++ks) {
+          const uint64_t dQh = ptx::smem_desc(base + ks * 32, 1024, 2);
+          const uint64_t dQl = ptx::smem_desc(base + A_BYTES + ks * 32, 1024, 2);
+          const uint64_t dK = ptx::smem_desc(base + 2 * A_BYTES + ks * 32, 1024, 2);
+          ptx::mma_f16(tmem, dQh, dK, idesc, (kb | ks) ? 1u : 0u);
+          ptx::mma_f16(tmem, dQl, dK, idesc, 1u);
+        }
+        ptx::mma_commit(&empty[s]);
+      }
+      ptx::mma_commit(accum);
+    }
+  } else {
+    const int quarter = warp & 3;
+    const int rl = quarter * 32 + lane;
+    const int r = r0 + rl;
+    const bool rok = r < a.R;
+    const float Tr = rok ? a.T[r] : 0.0f;
+    const float qs = rok ? a.qscale[r] : 0.0f;
+    const bool live = rok && Tr > 1e-10f;
+    if (ptx::mbar_wait(accum, 0, a.status, 6)) {
+      ptx::tc_fence_after();
+      const RotMat Rm = sR[rl];
+      const uint32_t lane_addr = tmem + ((uint32_t)(quarter * 32) << 16);
+      for (int c0 = 0; c0 < BN; c0 += 16) {
+        float u[16];
+        ptx::tmem_ld16(lane_addr + c0, u);
+        ptx::tmem_wait_ld();
+        if (!live) continue;
+#pragma unroll 4
+        for (int j = 0; j < 16; ++j) {
+          const int q = q0 + c0 + j;
+          if (q >= a.P_eff) break;
+          const float U = u[j] * qs;
+          const float slice = U / Tr;
+          tc_insert(a, Rm, __ldg(a.cx + q), __ldg(a.cy + q), __ldg(a.cz + q), Tr * slice, Tr);
+        }
+      }
+    }
+  }
+  ptx::tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    ptx::tc_fence_after();
+    ptx::tmem_dealloc(tmem, 256);
+  }
+}
+
+// Q = P c_i / phi (phi holds c_i num/den, the M-step multiplies raw
+// counts) as FP16 hi + lo, each rotation row scaled by 2^e_r so that its
+// largest entry sits near 2^14: qscale_r = 2^-e_r.
+__global__ void __launch_bounds__(256) tc_qsplit_kernel(const float* __restrict__ P,
+                                                        const float* __restrict__ PHI,
+                                                        const float* __restrict__ cnorm, int R, int N,
+                                                        int Np, __half* __restrict__ Qh,
+                                                        __half* __restrict__ Ql,
+                                                        float* __restrict__ qscale) {
+  const int r = blockIdx.x;
+  float mx = 0.0f;
+  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+    const size_t e = (size_t)r * N + i;
+    const float f = PHI[e];
+    const float q = f > 0.0f ? P[e] * __ldg(cnorm + i) / f : 0.0f;
+    mx = fmaxf(mx, q);
+  }
+  __shared__ float sm[256];
+  sm[threadIdx.x] = mx;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if (threadIdx.x < o) sm[threadIdx.x] = fmaxf(sm[threadIdx.x], sm[threadIdx.x + o]);
+    __syncthreads();
+  }
+  mx = sm[0];
+  int e = 0;
+  if (mx > 0.0f) e = 14 - ilogbf(mx) - 1;
+  e = max(-100, min(100, e));
+  const float up = ldexpf(1.0f, e);
+  for (int i = threadIdx.x; i < Np; i += blockDim.x) {
+    float q = 0.0f;
+    if (i < N) {
+      const size_t o = (size_t)r * N + i;
+      const float f = PHI[o];
+      q = f > 0.0f ? P[o] * __ldg(cnorm + i) / f * up : 0.0f;
+    }
+    const __half hi = __float2half_rn(q);
+    Qh[(size_t)r * Np + i] = hi;
+    Ql[(size_t)r * Np + i] = __float2half_rn(q - __half2float(hi));
+  }
+  if (threadIdx.x == 0) qscale[r] = ldexpf(1.0f, -e);
+}
+
+// ------------------------------------------------------------ host -------
+struct TcState {
+  CUtensorMap mK, mK2h, mK2l, mMp, mMS, mGh, mGl, mHh, mHl, mQh, mQl, mKt;
+  __half *Mp, *MSh, *Gh, *Gl, *Hh, *Hl;
+  float* qscale;
+  int* status;
+};
+
+static TcState* state(emc_plan* p) { return (TcState*)p->tc; }
+
+int tc_bind(emc_plan* p) {
+  emc_ctx* ctx = p->ctx;
+  if (!p->counts_fp16_exact)
+    return fail(ctx, EMC_ERR_UNSUPPORTED,
+                "mixed precision needs integer counts in [0, 2048] (exact in FP16)");
+  if (p->d.diff != EMC_DIFF_POISSON)
+    return fail(ctx, EMC_ERR_UNSUPPORTED, "mixed precision implements the reference poisson diff");
+  const int N = p->d.n_images, Np = p->Np, Kp = p->Kp, Rp = p->Rp;
+  int rc = EMC_OK;
+  if (!p->tc) {
+    TcState* st = new TcState();
+    std::memset(st, 0, sizeof(*st));
+    p->tc = st;
+    const size_t pk = (size_t)Np * Kp, rk = (size_t)Rp * Kp;
+    if (!rc) rc = plan_alloc(p, (void**)&p->Kh, pk * 2);
+    if (!rc) rc = plan_alloc(p, (void**)&p->K2hi, pk * 2);
+    if (!rc) rc = plan_alloc(p, (void**)&p->K2lo, pk * 2);
+    if (!rc) rc = plan_alloc(p, (void**)&p->KhT, pk * 2);
+    if (!rc) rc = plan_alloc(p, (void**)&p->k2lo_any, (size_t)(Np / 128) * (Kp / 32));
+    __half** rot_ops[6] = {&st->Mp, &st->MSh, &st->Gh, &st->Gl, &st->Hh, &st->Hl};
+    for (auto pp : rot_ops)
+      if (!rc) rc = plan_alloc(p, (void**)pp, rk * 2);
+    if (!rc) rc = plan_alloc(p, (void**)&p->Qh, (size_t)Rp * Np * 2);
+    if (!rc) rc = plan_alloc(p, (void**)&p->Ql, (size_t)Rp * Np * 2);
+    if (!rc) rc = plan_alloc(p, (void**)&st->qscale, (size_t)Rp * 4);
+    if (!rc) rc = plan_alloc(p, (void**)&st->status, 64);
+    if (rc) return rc;
+    EMC_CUDA(ctx, cudaMemsetAsync(p->Qh, 0, (size_t)Rp * Np * 2, ctx->stream));
+    EMC_CUDA(ctx, cudaMemsetAsync(p->Ql, 0, (size_t)Rp * Np * 2, ctx->stream));
+    // tensor maps (fixed addresses for the plan's lifetime)
+    if (!rc) rc = make_map(ctx, &st->mK, p->Kh, Np, Kp, 128, 32);
+    if (!rc) rc = make_map(ctx, &st->mK2h, p->K2hi, Np, Kp, 128, 32);
+    if (!rc) rc = make_map(ctx, &st->mK2l, p->K2lo, Np, Kp, 128, 32);
+    const __half* ro[6] = {st->Mp, st->MSh, st->Gh, st->Gl, st->Hh, st->Hl};
+    CUtensorMap* rm[6] = {&st->mMp, &st->mMS, &st->mGh, &st->mGl, &st->mHh, &st->mHl};
+    for (int j = 0; j < 6 && !rc; ++j) rc = make_map(ctx, rm[j], ro[j], Rp, Kp, 128, 32);
+    if (!rc) rc = make_map(ctx, &st->mQh, p->Qh, Rp, Np, 128, 64);
+    if (!rc) rc = make_map(ctx, &st->mQl, p->Ql, Rp, Np, 128, 64);
+    if (!rc) rc = make_map(ctx, &st->mKt, p->KhT, Kp, Np, 256, 64);
+    if (rc) return rc;
+    EMC_CUDA(ctx, cudaFuncSetAttribute(tc_estep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       es::SMEM_BYTES));
+    EMC_CUDA(ctx, cudaFuncSetAttribute(tc_mstep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       ms::SMEM_BYTES));
+  }
+  tc_pattern_ops_kernel<<<dim3(ceil_div(Kp, 256), Np), 256, 0, ctx->stream>>>(
+      p->images, p->pix, p->n2, N, Kp, p->Kh, p->K2hi, p->K2lo);
+  if ((rc = after_launch(ctx, "tc_pattern_ops_kernel"))) return rc;
+  tc_k2lo_flags_kernel<<<dim3(Kp / 32, Np / 128), 256, 0, ctx->stream>>>(p->K2lo, Kp, p->k2lo_any,
+                                                                         Kp / 32);
+  if ((rc = after_launch(ctx, "tc_k2lo_flags_kernel"))) return rc;
+  transpose_h_kernel<<<dim3(ceil_div(Kp, 32), ceil_div(Np, 32)), dim3(32, 8), 0, ctx->stream>>>(
+      p->Kh, Np, Kp, p->KhT);
+  return after_launch(ctx, "transpose_h_kernel");
+}
+
+static int check_status(emc_plan* p, const char* what) {
+  emc_ctx* ctx = p->ctx;
+  int h = 0, f = 0;
+  EMC_CUDA(ctx, cudaMemcpyAsync(&h, state(p)->status, sizeof(int), cudaMemcpyDeviceToHost,
+                                ctx->stream));
+  EMC_CUDA(ctx, cudaMemcpyAsync(&f, p->flags, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  EMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  if (h) return fail(ctx, EMC_ERR_TIMEOUT, "%s: pipeline wait timed out (status 0x%x)", what, h);
+  if (f & 4)
+    return fail(ctx, EMC_ERR_UNSUPPORTED, "%s: slice values exceed the FP16 operand range", what);
+  return EMC_OK;
+}
+
+int tc_estep(emc_plan* p, float sigma) {
+  emc_ctx* ctx = p->ctx;
+  TcState* st = state(p);
+  const size_t rk = (size_t)p->Rp * p->Kp;
+  int rc;
+  tc_rot_ops_kernel<<<ctx->sm_count * 8, 256, 0, ctx->stream>>>(p->S, rk, st->Mp, st->MSh, st->Gh,
+                                                                st->Gl, st->Hh, st->Hl, p->flags);
+  if ((rc = after_launch(ctx, "tc_rot_ops_kernel"))) return rc;
+  EMC_CUDA(ctx, cudaMemsetAsync(st->status, 0, sizeof(int), ctx->stream));
+  TcEstepArgs a;
+  a.N = p->d.n_images;
+  a.R = p->d.n_rot;
+  a.Kp = p->Kp;
+  a.n_pt = p->Np / es::BM;
+  a.n_rt = p->Rp / es::BN;
+  a.nkb = p->Kp / es::BK;
+  a.k2lo_any = p->k2lo_any;
+  a.rot_cnt = p->rot_cnt;
+  a.rot_A = p->rot_A;
+  a.rotw = p->rotw;
+  a.cnorm = p->cnorm;
+  a.inv2s2 = 1.0f / (2.0f * sigma * sigma);
+  a.known_intensity = p->d.known_intensity;
+  a.L = p->L;
+  a.PHI = p->PHI;
+  a.part = p->part;
+  a.bad = p->flags + 4;
+  a.status = st->status;
+  const int tiles = a.n_pt * a.n_rt;
+  tc_estep_kernel<<<tiles, es::THREADS, es::SMEM_BYTES, ctx->stream>>>(
+      st->mK, st->mK2h, st->mK2l, st->mMp, st->mMS, st->mGh, st->mGl, st->mHh, st->mHl, a);
+  if ((rc = after_launch(ctx, "tc_estep_kernel"))) return rc;
+  return EMC_OK;
+}
+
+int tc_mstep(emc_plan* p, float* model, float* weight) {
+  emc_ctx* ctx = p->ctx;
+  TcState* st = state(p);
+  int rc;
+  tc_qsplit_kernel<<<p->d.n_rot, 256, 0, ctx->stream>>>(p->L, p->PHI, p->cnorm, p->d.n_rot,
+                                                        p->d.n_images, p->Np, p->Qh, p->Ql,
+                                                        st->qscale);
+  if ((rc = after_launch(ctx, "tc_qsplit_kernel"))) return rc;
+  TcMstepArgs a;
+  a.R = p->d.n_rot;
+  a.Kp = p->Kp;
+  a.Np = p->Np;
+  a.P_eff = p->P_eff;
+  a.n_qt = p->Kp / ms::BN + (p->Kp % ms::BN ? 1 : 0);
+  a.n_rt = p->Rp / ms::BM;
+  a.nkb = p->Np / ms::BK;
+  a.T = p->T;
+  a.qscale = st->qscale;
+  a.rot = p->rot;
+  a.cx = p->cx;
+  a.cy = p->cy;
+  a.cz = p->cz;
+  a.side = p->d.side;
+  a.interp = p->d.interp;
+  a.deterministic = p->d.insert_mode == EMC_INSERT_DETERMINISTIC;
+  a.model = model;
+  a.weight = weight;
+  a.fix_m = p->fix_m;
+  a.fix_w = p->fix_w;
+  a.bounds = p->red + kRedBoundM;
+  a.status = st->status;
+  const int tiles = a.n_qt * a.n_rt;
+  tc_mstep_kernel<<<tiles, ms::THREADS, ms::SMEM_BYTES, ctx->stream>>>(st->mQh, st->mQl, st->mKt, a);
+  if ((rc = after_launch(ctx, "tc_mstep_kernel"))) return rc;
+  return check_status(p, "tensor-core iteration");
+}
+
+void tc_free(emc_plan* p) {
+  delete state(p);
+  p->tc = nullptr;
+}
+
 }  // namespace emc

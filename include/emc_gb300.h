@@ -213,7 +213,8 @@ size_t emc_plan_workspace_bytes(const emc_plan* plan);
 /* Binds the problem's device inputs (caller-owned, must outlive the plan's
  * use) and pre-processes the patterns (FP16 count operands, compaction to
  * the masked pixels).  images [N*s*s], mask [s*s], coords [s*s] x3,
- * rotations [4R], rotation weights [R]. */
+ * rotations [4R], rotation weights [R].  May be called again (new pattern
+ * data, same mask pixel count) without reallocating. */
 int emc_plan_bind(emc_plan* plan, const float* d_images, const int* d_mask, const float* d_x,
                   const float* d_y, const float* d_z, const float* d_rot,
                   const float* d_rot_weights);
@@ -223,6 +224,13 @@ int emc_plan_bind(emc_plan* plan, const float* d_images, const int* d_mask, cons
  * stats (host, may be NULL) is filled after a synchronise. */
 int emc_iterate(emc_plan* plan, float* d_model, float* d_weight, float sigma,
                 emc_iter_stats* stats);
+/* Instrumentation: with profiling on, emc_iterate records CUDA events on the
+ * context stream between its phases; emc_plan_phase_ms (after the iteration
+ * completes) returns the durations of expand, E-step (scaling + likelihood),
+ * log-sum-exp, responsibility normalisation, M-step (+ insertion) and the
+ * finishing model operations, in that order (n <= 6 values). */
+int emc_plan_set_profiling(emc_plan* plan, int on);
+int emc_plan_phase_ms(emc_plan* plan, float* ms, int n);
 /* Device pointers into the plan's workspace (valid until the next call):
  * the normalised responsibilities [R*N] (rotation-major) and scaling [R*N]
  * of the last iteration, and the per-pattern lse [N] (double). */

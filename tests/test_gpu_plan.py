@@ -78,6 +78,42 @@ def test_fp32_iteration_matches_fp64_oracle(ctx, cuda, prob, kw):
     assert abs(st.model_mean_before - want["mean_before"]) <= 1e-5 * want["mean_before"]
 
 
+MIXED_CASES = [
+    dict(interp=E.INTERP_NEAREST),
+    dict(interp=E.INTERP_TRILINEAR),
+    dict(interp=E.INTERP_NEAREST, normalize_images=1),
+    dict(interp=E.INTERP_NEAREST, known_intensity=1),
+    dict(interp=E.INTERP_NEAREST, insert_mode=E.INSERT_DETERMINISTIC),
+]
+
+
+@pytest.mark.parametrize("kw", MIXED_CASES, ids=lambda k: "-".join(f"{a}{b}" for a, b in k.items()))
+def test_mixed_iteration_matches_fp64_oracle(ctx, cuda, prob, kw):
+    """Tensor-core path (FP16 hi+lo operands, FP32 accumulation) against the
+    FP64 oracle: model relative L2 5e-4, log-likelihood relative 2e-5,
+    responsibilities absolute 1e-3, scaling relative 1e-4."""
+    sigma = 0.3
+    got = run_plan(ctx, prob, cuda, sigma=sigma, precision=E.PREC_MIXED, **kw)
+    want = O.fused_iteration_fp64(prob.init_model, prob.images, prob.mask, prob.x, prob.y, prob.z,
+                                  prob.quats, prob.weights, sigma, prob.cfg.side,
+                                  interp=kw["interp"],
+                                  known_intensity=bool(kw.get("known_intensity", 0)),
+                                  normalize_images=bool(kw.get("normalize_images", 0)))
+    st = got["stats"]
+    assert abs(st.total_loglik - want["total_loglik"]) <= 2e-5 * abs(want["total_loglik"])
+    assert np.abs(got["respons"] - want["respons"]).max() < 1e-3
+    np.testing.assert_allclose(got["phi"], want["phi"], rtol=1e-4)
+    assert rel_l2(got["model"], want["model"]) < 5e-4
+    assert rel_l2(got["weight"], want["weight"]) < 5e-4
+
+
+def test_mixed_rejects_non_integer_counts(ctx, cuda, prob):
+    p = S.Problem(**{**prob.__dict__})
+    p.images = prob.images + 0.5
+    with pytest.raises(E.EmcError, match="UNSUPPORTED"):
+        run_plan(ctx, p, cuda, precision=E.PREC_MIXED)
+
+
 def test_deterministic_insert_is_bit_identical(ctx, cuda, prob):
     a = run_plan(ctx, prob, cuda, insert_mode=E.INSERT_DETERMINISTIC)
     b = run_plan(ctx, prob, cuda, insert_mode=E.INSERT_DETERMINISTIC)

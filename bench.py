@@ -314,6 +314,17 @@ def run_ours(args):
                  "iter_per_s": 1e3 / ms_step, "note": "the measured path is the plain FP32 path"}
 
     # ---- end to end through the public API with host buffers
+    e2e = None
+    if args.e2e_steps > 0:
+        e2e = run_e2e(args, prob, plan, images, mask, x, y, z, rot, w, model, weight, sig,
+                      torch_stream, ws, pairs)
+    return finish(args, prob, plan, ctx, ws, rank, precision, value, ms_step, st, plain, e2e,
+                  estep_ms, phases, launches, clocks, pairs)
+
+
+def run_e2e(args, prob, plan, images, mask, x, y, z, rot, w, model, weight, sig, torch_stream, ws,
+            pairs):
+    import torch
     h_images = torch.from_numpy(prob.images).pin_memory()
     h_model = torch.from_numpy(prob.init_model).pin_memory()
     h_out_m = torch.empty_like(h_model).pin_memory()
@@ -327,7 +338,7 @@ def run_ours(args):
         images.copy_(h_images, non_blocking=True)
         model.copy_(h_model, non_blocking=True)
         plan.bind(images, mask, x, y, z, rot, w)
-        stk = plan.iterate(model, weight, sig[k])
+        stk = plan.iterate(model, weight, sig[k % len(sig)])
         h_out_m.copy_(model, non_blocking=True)
         h_out_w.copy_(weight, non_blocking=True)
         lls.append(stk.total_loglik)
@@ -336,11 +347,14 @@ def run_ours(args):
     wall = (time.perf_counter() - t0) / args.e2e_steps
     e2e_ms = max(e0.elapsed_time(e1) / args.e2e_steps, wall * 1e3)
     e2e_ms = max_over_ranks(ws, e2e_ms)
-    e2e = {"value": pairs * ws / (e2e_ms / 1e3), "unit": UNIT,
-           "h2d_bytes_per_step": int(prob.images.nbytes + prob.init_model.nbytes),
-           "d2h_bytes_per_step": int(2 * prob.init_model.nbytes + 8 * 4),
-           "ms_per_step": e2e_ms}
+    return {"value": pairs * ws / (e2e_ms / 1e3), "unit": UNIT,
+            "h2d_bytes_per_step": int(prob.images.nbytes + prob.init_model.nbytes),
+            "d2h_bytes_per_step": int(2 * prob.init_model.nbytes + 8 * 4),
+            "ms_per_step": e2e_ms}
 
+
+def finish(args, prob, plan, ctx, ws, rank, precision, value, ms_step, st, plain, e2e, estep_ms,
+           phases, launches, clocks, pairs):
     # ---- roofline of the dominant kernel (E-step)
     peaks = load_peaks()
     p_eff = int(prob.mask.sum())

@@ -85,6 +85,22 @@ def sigma_schedule(iteration: int, sigma_start: float, sigma_final: float, half_
     return float(_lib.load().emc_sigma_schedule(iteration, sigma_start, sigma_final, half_life))
 
 
+def read_config(path=None, text=None) -> "_lib.Config":
+    """emc.conf (configs.cpp:40-90 keys) -> emc_config; raises EmcError on a
+    syntax or type error."""
+    lib = _lib.load()
+    cfg = _lib.Config()
+    err = C.create_string_buffer(512)
+    if text is not None:
+        lib.emc_config_defaults(C.byref(cfg))
+        rc = lib.emc_config_parse(text.encode(), C.byref(cfg), err, 512)
+    else:
+        rc = lib.emc_config_read(str(path).encode(), C.byref(cfg), err, 512)
+    if rc != 0:
+        raise EmcError(f"config: {err.value.decode()}")
+    return cfg
+
+
 class Context:
     """One device, one stream (replaces cuda_set_device, emc_cuda.cu:867-870)."""
 

@@ -49,6 +49,24 @@ class IterStats(C.Structure):
     ]
 
 
+PATH_MAX = 512
+
+
+class Config(C.Structure):
+    """emc_config (the keys of the reference's Configuration)."""
+    _fields_ = [
+        ("model_side", I), ("read_stride", I), ("slice_chunk", I), ("N_images", I),
+        ("max_iterations", I), ("rotations_n", I), ("wavelength", D), ("pixel_size", D),
+        ("detector_size", I), ("detector_distance", D), ("sigma_start", D), ("sigma_final", D),
+        ("sigma_half_life", I), ("diff", I), ("blur_image", I), ("blur_sigma", D),
+        ("mask_file", C.c_char * PATH_MAX), ("image_prefix", C.c_char * PATH_MAX),
+        ("normalize_images", I), ("known_intensity", I), ("model_input", I),
+        ("model_file", C.c_char * PATH_MAX), ("exclude_images", I), ("exclude_ratio", D),
+        ("model_blur", D), ("isDebug", I), ("isOutput", I), ("output_loop", I),
+        ("output_period", I), ("nGPUs", I),
+    ]
+
+
 # name -> (restype, argtypes); every function declared in include/emc_gb300.h.
 SIGNATURES: dict[str, tuple] = {
     "emc_ctx_create": (I, [C.POINTER(P), I]),
@@ -79,6 +97,13 @@ SIGNATURES: dict[str, tuple] = {
     "emc_copy_real_to_device": (I, [P, P, P, I]),
     "emc_copy_real_to_host": (I, [P, P, P, I]),
     "emc_copy_real_d2d": (I, [P, P, P, I, I]),
+    "emc_copy_int_to_device": (I, [P, P, P, I]),
+    "emc_allocate_real": (I, [P, C.POINTER(P), C.c_size_t]),
+    "emc_allocate_int": (I, [P, C.POINTER(P), C.c_size_t]),
+    "emc_mem_free": (I, [P, P]),
+    "emc_config_defaults": (I, [P]),
+    "emc_config_parse": (I, [C.c_char_p, P, C.c_char_p, I]),
+    "emc_config_read": (I, [C.c_char_p, P, C.c_char_p, I]),
     "emc_plan_create": (I, [P, C.POINTER(PlanDesc), C.POINTER(P)]),
     "emc_plan_destroy": (I, [P]),
     "emc_plan_workspace_bytes": (C.c_size_t, [P]),
@@ -86,6 +111,7 @@ SIGNATURES: dict[str, tuple] = {
     "emc_iterate": (I, [P, P, P, F, C.POINTER(IterStats)]),
     "emc_plan_results": (I, [P, C.POINTER(P), C.POINTER(P), C.POINTER(P)]),
     "emc_plan_set_profiling": (I, [P, I]),
+    "emc_tc_gemm_selftest": (I, [P, P, P, P, I, I]),
     "emc_plan_phase_ms": (I, [P, P, I]),
 }
 

@@ -115,6 +115,41 @@ extern "C" int emc_copy_real_d2d(emc_ctx* ctx, float* d_dst, const float* d_src,
   return EMC_OK;
 }
 
+extern "C" int emc_copy_int_to_device(emc_ctx* ctx, const int* h_src, int* d_dst, int n) {
+  EMC_CHECK_CTX(ctx);
+  EMC_REQUIRE(ctx, n >= 0 && (n == 0 || (h_src && d_dst)), "copy_int_to_device: bad buffer");
+  if (n == 0) return EMC_OK;
+  EMC_CUDA(ctx, cudaMemcpyAsync(d_dst, h_src, sizeof(int) * (size_t)n, cudaMemcpyHostToDevice,
+                                ctx->stream));
+  return EMC_OK;
+}
+
+extern "C" int emc_allocate_real(emc_ctx* ctx, float** d_out, size_t n) {
+  EMC_CHECK_CTX(ctx);
+  EMC_REQUIRE(ctx, d_out, "allocate_real: null output");
+  *d_out = nullptr;
+  cudaError_t e = cudaMalloc((void**)d_out, sizeof(float) * (n ? n : 1));
+  if (e != cudaSuccess) return emc::fail(ctx, EMC_ERR_NOMEM, "allocate_real(%zu): %s", n, cudaGetErrorString(e));
+  return EMC_OK;
+}
+
+extern "C" int emc_allocate_int(emc_ctx* ctx, int** d_out, size_t n) {
+  EMC_CHECK_CTX(ctx);
+  EMC_REQUIRE(ctx, d_out, "allocate_int: null output");
+  *d_out = nullptr;
+  cudaError_t e = cudaMalloc((void**)d_out, sizeof(int) * (n ? n : 1));
+  if (e != cudaSuccess) return emc::fail(ctx, EMC_ERR_NOMEM, "allocate_int(%zu): %s", n, cudaGetErrorString(e));
+  return EMC_OK;
+}
+
+extern "C" int emc_mem_free(emc_ctx* ctx, void* d_ptr) {
+  EMC_CHECK_CTX(ctx);
+  if (!d_ptr) return EMC_OK;
+  EMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  EMC_CUDA(ctx, cudaFree(d_ptr));
+  return EMC_OK;
+}
+
 // main.cpp:251 -- the annealing width of iteration t.
 extern "C" float emc_sigma_schedule(int iteration, double sigma_start, double sigma_final,
                                     int half_life) {

@@ -168,3 +168,4 @@ extern "C" int emc_log_sum_max(emc_ctx* ctx, const float* d_sum, const float* d_
                                                                                 d_lse, N_images);
   return emc::after_launch(ctx, "log_sum_max_kernel");
 }
+

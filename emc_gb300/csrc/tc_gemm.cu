@@ -746,4 +746,113 @@ void tc_free(emc_plan* p) {
   p->tc = nullptr;
 }
 
+// ------------------------------------------------------- self-test -------
+// One CTA computes D[128 x BN] = A[128 x K] B[BN x K]^T with the same TMA,
+// shared-memory descriptor, MMA and TMEM-load code as the iteration kernels,
+// for the tile shapes they use: (BN = 128, 64B swizzle, 32-wide k-blocks)
+// and (BN = 256, 128B swizzle, 64-wide k-blocks).  Single-stage pipeline.
+template <int BN, int BK>
+__global__ void __launch_bounds__(128, 1)
+    tc_gemm_selftest_kernel(const __grid_constant__ CUtensorMap mA,
+                            const __grid_constant__ CUtensorMap mB, int K, float* D, int* status) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  constexpr int A_BYTES = 128 * BK * 2, B_BYTES = BN * BK * 2;
+  constexpr uint32_t SW = BK == 64 ? 2 : 4;
+  constexpr uint32_t SBO = BK * 2 * 8;
+  uint64_t* full = (uint64_t*)(smem + A_BYTES + B_BYTES);
+  uint64_t* done = full + 1;
+  uint32_t* tslot = (uint32_t*)(done + 1);
+  const int warp = threadIdx.x >> 5;
+  if (threadIdx.x == 0) {
+    ptx::mbar_init(full, 1);
+    ptx::mbar_init(done, 1);
+    ptx::fence_mbar_init();
+  }
+  if (warp == 0) {
+    ptx::tmem_alloc(tslot, BN);
+    ptx::tmem_relinquish();
+  }
+  ptx::tc_fence_before();
+  __syncthreads();
+  ptx::tc_fence_after();
+  const uint32_t tmem = *tslot;
+  bool ok = true;
+  for (int kb = 0; kb < K / BK && ok; ++kb) {
+    if (threadIdx.x == 0) {
+      ptx::mbar_arrive_expect_tx(full, A_BYTES + B_BYTES);
+      ptx::tma_load_2d(smem, &mA, kb * BK, 0, full);
+      ptx::tma_load_2d(smem + A_BYTES, &mB, kb * BK, 0, full);
+    }
+    ok = ptx::mbar_wait(full, kb & 1, status, 0);
+    ptx::tc_fence_after();
+    if (threadIdx.x == 0 && ok) {
+      const uint32_t base = ptx::smem_u32(smem);
+      for (int ks = 0; ks < BK / 16; ++ks)
+        ptx::mma_f16(tmem, ptx::smem_desc(base + ks * 32, SBO, SW),
+                     ptx::smem_desc(base + A_BYTES + ks * 32, SBO, SW), ptx::idesc_f16(128, BN),
+                     (kb | ks) ? 1u : 0u);
+      ptx::mma_commit(done);
+    }
+    if (ok) ok = ptx::mbar_wait(done, kb & 1, status, 1);
+    ptx::tc_fence_after();
+    __syncthreads();
+  }
+  if (ok) {
+    const int q = warp & 3;
+    const uint32_t la = tmem + ((uint32_t)(q * 32) << 16);
+    const int row = q * 32 + (threadIdx.x & 31);
+    for (int c0 = 0; c0 < BN; c0 += 16) {
+      float v[16];
+      ptx::tmem_ld16(la + c0, v);
+      ptx::tmem_wait_ld();
+      for (int j = 0; j < 16; ++j) D[(size_t)row * BN + c0 + j] = v[j];
+    }
+  }
+  ptx::tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    ptx::tc_fence_after();
+    ptx::tmem_dealloc(tmem, BN);
+  }
+}
+
 }  // namespace emc
+
+// Diagnostic: D[128 x n] = A[128 x k] B[n x k]^T (FP16 in, FP32 out, device
+// pointers) through the tcgen05 building blocks; n = 128 uses the E-step's
+// 64B-swizzled 32-wide k-blocks, n = 256 the M-step's 128B-swizzled 64-wide
+// k-blocks.  k must be a multiple of the k-block.
+extern "C" int emc_tc_gemm_selftest(emc_ctx* ctx, const void* d_a, const void* d_b, float* d_d,
+                                    int n, int k) {
+  using namespace emc;
+  EMC_CHECK_CTX(ctx);
+  EMC_REQUIRE(ctx, d_a && d_b && d_d, "tc_gemm_selftest: null pointer");
+  EMC_REQUIRE(ctx, n == 128 || n == 256, "tc_gemm_selftest: n must be 128 or 256");
+  const int bk = n == 128 ? 32 : 64;
+  EMC_REQUIRE(ctx, k > 0 && k % bk == 0, "tc_gemm_selftest: k %% %d != 0", bk);
+  CUtensorMap mA, mB;
+  int rc = make_map(ctx, &mA, d_a, 128, k, 128, bk);
+  if (!rc) rc = make_map(ctx, &mB, d_b, n, k, n, bk);
+  if (rc) return rc;
+  int* status = nullptr;
+  EMC_CUDA(ctx, cudaMallocAsync((void**)&status, sizeof(int), ctx->stream));
+  EMC_CUDA(ctx, cudaMemsetAsync(status, 0, sizeof(int), ctx->stream));
+  const int smem = 128 * bk * 2 + n * bk * 2 + 1024 + 1024;
+  if (n == 128) {
+    EMC_CUDA(ctx, cudaFuncSetAttribute(tc_gemm_selftest_kernel<128, 32>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    tc_gemm_selftest_kernel<128, 32><<<1, 128, smem, ctx->stream>>>(mA, mB, k, d_d, status);
+  } else {
+    EMC_CUDA(ctx, cudaFuncSetAttribute(tc_gemm_selftest_kernel<256, 64>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    tc_gemm_selftest_kernel<256, 64><<<1, 128, smem, ctx->stream>>>(mA, mB, k, d_d, status);
+  }
+  if ((rc = after_launch(ctx, "tc_gemm_selftest_kernel"))) return rc;
+  int h = 0;
+  EMC_CUDA(ctx, cudaMemcpyAsync(&h, status, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  EMC_CUDA(ctx, cudaFreeAsync(status, ctx->stream));
+  EMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  if (h) return fail(ctx, EMC_ERR_TIMEOUT, "tc_gemm_selftest: wait timed out (0x%x)", h);
+  return EMC_OK;
+}

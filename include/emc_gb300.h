@@ -92,6 +92,35 @@ int emc_calculate_coordinates(int side, float pixel_size, float detector_distanc
 /* main.cpp:251: sigma_t = sf + (ss - sf) * exp(-t / half_life * ln 2). */
 float emc_sigma_schedule(int iteration, double sigma_start, double sigma_final, int half_life);
 
+/* ---- configuration (emc.conf) ------------------------------------------ */
+/* The keys of Configuration (configs.h:11-89) read by configs.cpp:40-90. */
+#define EMC_CONFIG_PATH_MAX 512
+typedef struct {
+  int model_side, read_stride, slice_chunk, N_images, max_iterations, rotations_n;
+  double wavelength, pixel_size;
+  int detector_size;
+  double detector_distance, sigma_start, sigma_final;
+  int sigma_half_life;
+  int diff; /* EMC_DIFF_* from diff_type */
+  int blur_image;
+  double blur_sigma;
+  char mask_file[EMC_CONFIG_PATH_MAX];
+  char image_prefix[EMC_CONFIG_PATH_MAX];
+  int normalize_images, known_intensity, model_input;
+  char model_file[EMC_CONFIG_PATH_MAX];
+  int exclude_images;
+  double exclude_ratio, model_blur;
+  int isDebug, isOutput, output_loop, output_period, nGPUs;
+} emc_config;
+/* emc.conf's own values (emc.conf:1-26), nGPU 1, and 0 for the keys emc.conf
+ * leaves out (the reference leaves those uninitialised). */
+int emc_config_defaults(emc_config* c);
+/* Config::read_configuration_file (configs.cpp:40-90) without libconfig:
+ * parses libconfig-syntax text over *c (call emc_config_defaults first);
+ * EMC_ERR_INVALID with a message in err on a syntax or type error. */
+int emc_config_parse(const char* text, emc_config* c, char* err, int errlen);
+int emc_config_read(const char* path, emc_config* c, char* err, int errlen);
+
 /* ---- per-function drop-ins (reference semantics) ----------------------- */
 /* cuda_get_slices (emc_cuda_help.h:47-49; emc_cuda.cu:102-157, 542-560):
  * slices[r] for rotations start_slice .. start_slice+slice_chunk-1 of d_rot.
@@ -181,6 +210,15 @@ int emc_reset_real(emc_ctx* ctx, float* d_real, int len);
 int emc_copy_real_to_device(emc_ctx* ctx, const float* h_src, float* d_dst, int n);
 int emc_copy_real_to_host(emc_ctx* ctx, float* h_dst, const float* d_src, int n);
 int emc_copy_real_d2d(emc_ctx* ctx, float* d_dst, const float* d_src, int start, int n);
+/* cuda_copy_int_to_device (emc_cuda_help.h:99; emc_cuda.cu:913-915). */
+int emc_copy_int_to_device(emc_ctx* ctx, const int* h_src, int* d_dst, int n);
+
+/* cuda_allocate_real / cuda_allocate_int / cuda_mem_free (emc_cuda_help.h:73-74,
+ * 93; emc_cuda.cu:872-878, 1274-1279): device buffers for a host that drives
+ * the drop-in entry points through this ABI only (e.g. the `emc` driver). */
+int emc_allocate_real(emc_ctx* ctx, float** d_out, size_t n);
+int emc_allocate_int(emc_ctx* ctx, int** d_out, size_t n);
+int emc_mem_free(emc_ctx* ctx, void* d_ptr);
 
 /* ---- fused iteration (the fast path) ----------------------------------- */
 typedef struct {
@@ -231,6 +269,11 @@ int emc_iterate(emc_plan* plan, float* d_model, float* d_weight, float sigma,
  * finishing model operations, in that order (n <= 6 values). */
 int emc_plan_set_profiling(emc_plan* plan, int on);
 int emc_plan_phase_ms(emc_plan* plan, float* ms, int n);
+/* Diagnostic of the tensor-core building blocks (TMA, shared-memory
+ * descriptors, tcgen05.mma, TMEM loads): D[128 x n] = A[128 x k] B[n x k]^T,
+ * FP16 A and B (row-major, device), FP32 D.  n = 128 exercises the E-step
+ * tile shape, n = 256 the M-step's.  No counterpart in the reference. */
+int emc_tc_gemm_selftest(emc_ctx* ctx, const void* d_a, const void* d_b, float* d_d, int n, int k);
 /* Device pointers into the plan's workspace (valid until the next call):
  * the normalised responsibilities [R*N] (rotation-major) and scaling [R*N]
  * of the last iteration, and the per-pattern lse [N] (double). */

@@ -42,10 +42,17 @@ gcc -O2 -std=gnu99 -w -I"$here/shim" -I"$ref" -include stdio.h -include stdlib.h
     "$ref/rotations.c" "$here/ref_rotations_main.c" "$here/shim/spimage_stubs.c" -lm \
     -o "$out/ref_rotations"
 if [[ $want_kernels == 1 ]]; then
-  nvcc -std=c++17 -O3 -gencode arch=compute_103a,code=sm_103a -Xcompiler -fPIC -shared -w \
-      -I"$here/shim" -I"$ref" -DcudaThreadSynchronize=cudaDeviceSynchronize \
-      -include thrust/transform_reduce.h \
-      "$here/ref_harness.cu" "$here/shim/spimage_stubs.c" -lcufft \
-      -o "$out/libemc_ref_kernels.so"
+  # emc_cuda.cu and emc_atomic.cu each define inblock_reduce, so they are
+  # separate translation units, as in the reference's own build.
+  flags=(-std=c++17 -O3 -gencode arch=compute_103a,code=sm_103a -Xcompiler -fPIC -w
+         -I"$here/shim" -I"$ref" -DcudaThreadSynchronize=cudaDeviceSynchronize
+         -include thrust/transform_reduce.h)
+  nvcc "${flags[@]}" -c "$ref/emc_cuda.cu" -o "$out/emc_cuda.o" &
+  nvcc "${flags[@]}" -c "$ref/emc_atomic.cu" -o "$out/emc_atomic.o" &
+  nvcc "${flags[@]}" -c "$here/ref_harness.cu" -o "$out/ref_harness.o" &
+  wait
+  gcc -O2 -fPIC -c -I"$here/shim" "$here/shim/spimage_stubs.c" -o "$out/spimage_stubs.o"
+  nvcc -shared -gencode arch=compute_103a,code=sm_103a "$out/emc_cuda.o" "$out/emc_atomic.o" \
+      "$out/ref_harness.o" "$out/spimage_stubs.o" -lcufft -o "$out/libemc_ref_kernels.so"
 fi
 echo "built reference checker in $out"

@@ -269,14 +269,41 @@ def fused_iteration_fp64(model, images, mask, x, y, z, quats, weights, sigma, si
         lse = np.where(np.isfinite(Mx), Mx + np.log(np.exp(Lr - Mx[None, :]).sum(0)), np.inf)
         P = np.where(np.isfinite(lse)[None, :], np.exp(Lr - lse[None, :]), 0.0)
     P = np.nan_to_num(P)
+    m = mstep_fp64(P, phi, K, xs, ys, zs, quats, side, interp, blur_sigma)
+    total_ll = float(lse[np.isfinite(lse)].sum())
+    return dict(model=m["model"], weight=m["weight"], respons=P, phi=phi, loglik=Lr, lse=lse,
+                total_loglik=total_ll, T=m["T"], mean_before=m["mean_before"])
+
+
+def compacted_counts(images, mask, side, normalize_images=False):
+    """The M-step's pattern operand: counts at the mask pixels (times the
+    reference's per-pattern factor when normalising), FP64 [N, P_eff]."""
+    images = np.asarray(images, np.float64)
+    pix = _compact(mask)
+    if normalize_images:
+        c = (np.float32(side * side) / images[:, pix].astype(np.float32).sum(1, dtype=np.float32))
+        return (images[:, pix].astype(np.float32) * c.astype(np.float32)[:, None]).astype(np.float64)
+    return images[:, pix]
+
+
+def mstep_fp64(P, phi, K, xs, ys, zs, quats, side, interp=0, blur_sigma=0.0):
+    """M-step of the fused iteration from given responsibilities P [R, N] and
+    scaling phi [R, N]: U = (P/phi) K, insertion of T_r (U/T_r) with weight
+    T_r (rotations with T_r > 1e-10), divide, normalise to mean 1, blur."""
+    P = np.asarray(P, np.float64)
+    phi = np.asarray(phi, np.float64)
     with np.errstate(divide="ignore", invalid="ignore"):
         Qm = np.where(phi > 0, P / np.where(phi > 0, phi, 1.0), 0.0)
-    T = P.sum(1)
+    # T_r is summed in FP64 and kept as a float, and the live test is the
+    # float comparison T_r > 1e-10f, exactly as in the kernels (a rotation
+    # whose total sits at the threshold must decide the same way)
+    T32 = P.sum(1).astype(np.float32)
+    T = T32.astype(np.float64)
     U = Qm @ K  # [R, P_eff]
     n3 = side ** 3
     new_m = np.zeros(n3)
     new_w = np.zeros(n3)
-    live = T > 1e-10
+    live = T32 > np.float32(1e-10)
     if interp == 0:
         vox = nearest_voxels(quats, xs, ys, zs, side, 0)
         sel = (vox >= 0) & live[:, None]
@@ -296,9 +323,7 @@ def fused_iteration_fp64(model, images, mask, x, y, z, quats, weights, sigma, si
     out = out * (1.0 / mean)
     if blur_sigma > 0:
         out = blur_fft_fp64(out, side, blur_sigma)
-    total_ll = float(lse[np.isfinite(lse)].sum())
-    return dict(model=out, weight=new_w, respons=P, phi=phi, loglik=Lr, lse=lse,
-                total_loglik=total_ll, T=T, mean_before=mean)
+    return dict(model=out, weight=new_w, T=T, mean_before=mean)
 
 
 def blur_fft_fp64(model, side, sigma):

@@ -224,6 +224,41 @@ def test_degenerate_inputs_follow_reference(ctx, cuda):
     assert np.isnan(resp[2:]).all()
 
 
+def test_against_reference_kernel_golden(ctx, cuda):
+    """The drop-ins against the reference's own kernels (run on a GB300,
+    tests/golden/ref_kernels_golden.npz): bit-exact slicing, scaling and
+    M-step slices, likelihood within one float ulp."""
+    import os
+    G = np.load(os.path.join(os.path.dirname(__file__), "golden", "ref_kernels_golden.npz"))
+    s = int(G["side"])
+    q = G["quats"]
+    R, N = q.shape[0], G["images"].shape[0]
+    d = {k: T(G[k], cuda) for k in ("model", "x", "y", "z", "quats", "weights", "images")}
+    mask = T(G["mask"], cuda, torch.int32)
+    sl = torch.empty((R, s * s), device=cuda)
+    ctx.get_slices(d["model"], s, sl, d["quats"], d["x"], d["y"], d["z"], 0, R)
+    scal = torch.ones((R, N), device=cuda)
+    ctx.update_scaling_full(d["images"], sl, mask, scal, s * s, N, 0, R)
+    resp = torch.zeros((R, N), device=cuda)
+    ctx.calculate_responsabilities(sl, d["images"], mask, 0.3, scal, resp, d["weights"], s * s, N,
+                                   0, R)
+    upd = torch.zeros((60, s * s), device=cuda)
+    m = torch.zeros(s ** 3, device=cuda)
+    w = torch.zeros(s ** 3, device=cuda)
+    ctx.update_slices(d["images"], upd, mask, T(G["respons_norm"], cuda), scal,
+                      T(np.ones(N, np.int32), cuda, torch.int32), N, 16, 60, s * s, s, m, d["x"],
+                      d["y"], d["z"], d["quats"][16:76].contiguous(), w)
+    ctx.sync()
+    assert np.array_equal(sl.cpu().numpy(), G["slices"])
+    assert np.array_equal(scal.cpu().numpy(), G["scaling"], equal_nan=True)
+    np.testing.assert_allclose(resp.cpu().numpy(), G["respons_poisson"], rtol=2.4e-7)
+    assert np.array_equal(upd.cpu().numpy(), G["upd_slices"])
+    np.testing.assert_allclose(m.cpu().numpy(), G["ins_model"], rtol=1e-6,
+                               atol=1e-6 * G["ins_model"].max())
+    np.testing.assert_allclose(w.cpu().numpy(), G["ins_weight"], rtol=1e-6,
+                               atol=1e-6 * G["ins_weight"].max())
+
+
 def test_bad_arguments_raise(ctx, cuda):
     z = torch.zeros(16, device=cuda)
     with pytest.raises(E.EmcError):

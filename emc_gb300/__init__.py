@@ -277,6 +277,10 @@ class Plan:
         return st if stats else None
 
     PHASES = ("expand", "estep", "lse", "mprep", "mstep", "finish")
+    OPT_ESTEP_CLUSTER = 1
+
+    def set_option(self, option: int, value: int):
+        self.ctx._check(self._lib.emc_plan_set_option(self._h, option, value), "plan_set_option")
 
     def set_profiling(self, on: bool = True):
         self.ctx._check(self._lib.emc_plan_set_profiling(self._h, int(on)), "plan_set_profiling")

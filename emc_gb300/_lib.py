@@ -111,6 +111,7 @@ SIGNATURES: dict[str, tuple] = {
     "emc_iterate": (I, [P, P, P, F, C.POINTER(IterStats)]),
     "emc_plan_results": (I, [P, C.POINTER(P), C.POINTER(P), C.POINTER(P)]),
     "emc_plan_set_profiling": (I, [P, I]),
+    "emc_plan_set_option": (I, [P, I, I]),
     "emc_tc_gemm_selftest": (I, [P, P, P, P, I, I]),
     "emc_plan_phase_ms": (I, [P, P, I]),
 }

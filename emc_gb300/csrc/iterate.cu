@@ -23,6 +23,7 @@
 // no overlap (count_r == 0) or undefined scaling (num or den <= 0) get
 // L = -inf and phi = 1, a pattern whose pairs are all invalid gets zero
 // responsibility, and the normaliser is FP64.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -96,7 +97,7 @@ __global__ void pattern_ops_kernel(const float* __restrict__ images, const int* 
   }
   const size_t o = (size_t)i * Kp + q;
   Kraw[o] = k;
-  const float kt = (double)k > 1e-10 ? k : 0.0f;
+  const float kt = k >= 1e-10f ? k : 0.0f;  // the reference's (double)k > 1e-10
   if (Kt) Kt[o] = kt;
   if (K2) K2[o] = __fmul_rn(kt, kt);
 }
@@ -175,23 +176,24 @@ __global__ void __launch_bounds__(256) slice_rows_kernel(
   if (threadIdx.x == 0) sR = quat_to_matrix(rot + 4 * (size_t)r);
   __syncthreads();
   const RotMat Rm = sR;
-  double cnt = 0.0, A = 0.0, ss = 0.0;
+  // per-thread FP32 partials (FP64 arithmetic is scarce on this GPU), block sums in FP64
+  float cnt = 0.0f, A = 0.0f, ss = 0.0f;
   for (int q = threadIdx.x; q < Kp; q += blockDim.x) {
     float s = 0.0f;
     if (__ldg(pix + q) >= 0) {
       s = plan_sample<INTERP>(model, side, Rm, __ldg(cx + q), __ldg(cy + q), __ldg(cz + q));
       if (s > 0.0f) {
-        cnt += 1.0;
-        A += (double)s * s / ((double)s + kPoisC);
+        cnt += 1.0f;
+        A += s * s / (s + kPoisC);
       }
-      ss += (double)fmaxf(s, kSliceFloor);
+      ss += fmaxf(s, kSliceFloor);
     }
     S[(size_t)r * Kp + q] = s;
   }
   __shared__ double sh[3][256];
-  sh[0][threadIdx.x] = cnt;
-  sh[1][threadIdx.x] = A;
-  sh[2][threadIdx.x] = ss;
+  sh[0][threadIdx.x] = (double)cnt;
+  sh[1][threadIdx.x] = (double)A;
+  sh[2][threadIdx.x] = (double)ss;
   __syncthreads();
   for (int o = blockDim.x / 2; o > 0; o >>= 1) {
     if (threadIdx.x < o) {
@@ -354,8 +356,9 @@ __global__ void __launch_bounds__(TPB, 1) estep_fp32_kernel(EstepArgs a) {
     ld_tile(a.K2, a.Kp, n0, a.N, 0, vk2);
     ld_tile(a.Kt, a.Kp, n0, a.N, 0, vkt);
     for (int kb = 0; kb < nk; ++kb) {
-      st_tile_t(s0, vr, [](float s) { return (double)s > 1e-10 ? 1.0f : 0.0f; });
-      st_tile_t(s1, vr, [](float s) { return (double)s > 1e-10 ? s : 0.0f; });
+      // s >= 1e-10f is the reference's (double)s > 1e-10 for every float s
+      st_tile_t(s0, vr, [](float s) { return s >= 1e-10f ? 1.0f : 0.0f; });
+      st_tile_t(s1, vr, [](float s) { return s >= 1e-10f ? s : 0.0f; });
       st_tile_t(s2, vk2, [](float v) { return v; });
       st_tile_t(s3, vkt, [](float v) { return v; });
       __syncthreads();
@@ -558,43 +561,52 @@ __global__ void finite_sum_kernel(const double* __restrict__ x, int n, double* _
   if (threadIdx.x == 0) out[0] = sh[0];
 }
 
-// One block per rotation row: P = exp(L - lse) (in place), Q = P / phi
-// (row stride ldq, zero padded), T_r = sum_i P, and the row's captured mass
-// and inserted-mass bound sum_i Q_ri K_i (FP64).
-__global__ void __launch_bounds__(256) mprep_kernel(float* __restrict__ L,
-                                                    const float* __restrict__ PHI,
-                                                    const double* __restrict__ lse,
-                                                    const float* __restrict__ Ksum, int R, int N,
-                                                    float* __restrict__ Q, int ldq,
-                                                    float* __restrict__ T,
-                                                    double* __restrict__ row_mass,
-                                                    double* __restrict__ row_bound) {
+// One block per rotation row: P = exp(L - lse) (in place), Q = P / phi,
+// T_r = sum_i P, the row's captured mass and the inserted-mass bound
+// sum_i Q_ri K_i.  Element math is FP32 (expf of an FP64 difference, since
+// FP64 arithmetic is scarce on this GPU); per-thread sums are FP32 and the
+// block sums FP64.
+//   FP32 M-step: Q [R][ldq] (zero padded).
+//   Tensor M-step (Qh != nullptr): Q' = P c_i / phi (phi holds c_i num/den,
+//   the tensor M-step multiplies raw counts) as FP16 hi + lo [R][ldq], each
+//   row scaled by 2^e_r so its largest entry sits near 2^14 (qscale_r =
+//   2^-e_r); the second pass re-reads the row while it is in L2.
+__global__ void __launch_bounds__(256) mprep_kernel(
+    float* __restrict__ L, const float* __restrict__ PHI, const double* __restrict__ lse,
+    const float* __restrict__ Ksum, const float* __restrict__ cnorm, int R, int N,
+    float* __restrict__ Q, __half* __restrict__ Qh, __half* __restrict__ Ql,
+    float* __restrict__ qscale, int ldq, float* __restrict__ T, double* __restrict__ row_mass,
+    double* __restrict__ row_bound) {
   const int r = blockIdx.x;
-  double t = 0.0, b = 0.0;
-  for (int i = threadIdx.x; i < ldq; i += blockDim.x) {
-    float q = 0.0f;
-    if (i < N) {
-      const size_t e = (size_t)r * N + i;
-      const double li = lse[i];
-      const float l = L[e];
-      float P = 0.0f;
-      if (isfinite(li) && l > -INFINITY) P = (float)exp((double)l - li);
-      L[e] = P;
-      const float f = PHI[e];
-      q = f > 0.0f ? __fdiv_rn(P, f) : 0.0f;
-      t += (double)P;
-      b += (double)q * (double)__ldg(Ksum + i);
-    }
+  float t = 0.0f, b = 0.0f, qmax = 0.0f;
+  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+    const size_t e = (size_t)r * N + i;
+    const double li = lse[i];
+    const float l = L[e];
+    float P = 0.0f;
+    if (isfinite(li) && l > -INFINITY) P = expf((float)((double)l - li));
+    L[e] = P;
+    const float f = PHI[e];
+    float q = f > 0.0f ? __fdiv_rn(P, f) : 0.0f;
+    t += P;
+    b = __fmaf_rn(q, __ldg(Ksum + i), b);
+    if (Qh) q = __fmul_rn(q, __ldg(cnorm + i));
+    qmax = fmaxf(qmax, q);
     if (Q) Q[(size_t)r * ldq + i] = q;
   }
+  if (Q)
+    for (int i = N + threadIdx.x; i < ldq; i += blockDim.x) Q[(size_t)r * ldq + i] = 0.0f;
   __shared__ double sh[2][256];
-  sh[0][threadIdx.x] = t;
-  sh[1][threadIdx.x] = b;
+  __shared__ float smx[256];
+  sh[0][threadIdx.x] = (double)t;
+  sh[1][threadIdx.x] = (double)b;
+  smx[threadIdx.x] = qmax;
   __syncthreads();
   for (int o = blockDim.x / 2; o > 0; o >>= 1) {
     if (threadIdx.x < o) {
       sh[0][threadIdx.x] += sh[0][threadIdx.x + o];
       sh[1][threadIdx.x] += sh[1][threadIdx.x + o];
+      smx[threadIdx.x] = fmaxf(smx[threadIdx.x], smx[threadIdx.x + o]);
     }
     __syncthreads();
   }
@@ -603,6 +615,23 @@ __global__ void __launch_bounds__(256) mprep_kernel(float* __restrict__ L,
     row_mass[r] = sh[0][0];
     row_bound[r] = sh[1][0];
   }
+  if (!Qh) return;
+  const float mx = smx[0];
+  int ex = mx > 0.0f ? 14 - ilogbf(mx) - 1 : 0;
+  ex = max(-100, min(100, ex));
+  const float up = ldexpf(1.0f, ex);
+  for (int i = threadIdx.x; i < ldq; i += blockDim.x) {
+    float q = 0.0f;
+    if (i < N) {
+      const size_t e = (size_t)r * N + i;
+      const float f = PHI[e];
+      q = f > 0.0f ? __fmul_rn(__fmul_rn(__fdiv_rn(L[e], f), __ldg(cnorm + i)), up) : 0.0f;
+    }
+    const __half hi = __float2half_rn(q);
+    Qh[(size_t)r * ldq + i] = hi;
+    Ql[(size_t)r * ldq + i] = __float2half_rn(q - __half2float(hi));
+  }
+  if (threadIdx.x == 0) qscale[r] = ldexpf(1.0f, -ex);
 }
 
 // ---------------------------------------------------------- insert -------
@@ -823,7 +852,7 @@ extern "C" int emc_plan_create(emc_ctx* ctx, const emc_plan_desc* desc, emc_plan
   p->ctx = ctx;
   p->d = d;
   p->n2 = d.side * d.side;
-  p->Np = ceil_div(d.n_images, 128) * 128;
+  p->Np = ceil_div(d.n_images, 512) * 512;  // whole clusters of up to 4 pattern tiles
   p->Rp = ceil_div(d.n_rot, 128) * 128;
   p->n_rt = ceil_div(d.n_rot, EMC_RT);
   const size_t RN = (size_t)d.n_rot * d.n_images;
@@ -887,6 +916,18 @@ extern "C" int emc_plan_bind(emc_plan* p, const float* d_images, const int* d_ma
     if (hmask[q]) pix.push_back(q);
   }
   EMC_REQUIRE(ctx, !pix.empty(), "plan_bind: mask is empty");
+  // Compacted pixels in order of detector radius: the bright low-q pixels,
+  // the only ones whose k^2 needs a second FP16 term, then share a few
+  // k-blocks of the tensor-core E-step (the order is otherwise free: every
+  // compacted array uses it consistently).
+  {
+    const int side = p->d.side;
+    auto r2 = [side](int q) {
+      const double dx = (double)(q % side) - side / 2 + 0.5, dy = (double)(q / side) - side / 2 + 0.5;
+      return dx * dx + dy * dy;
+    };
+    std::stable_sort(pix.begin(), pix.end(), [&](int a, int b) { return r2(a) < r2(b); });
+  }
   EMC_REQUIRE(ctx, prev_P == 0 || prev_P == (int)pix.size(),
               "plan_bind: a re-bind must keep the mask's pixel count (%d != %d)", (int)pix.size(),
               prev_P);
@@ -1055,9 +1096,11 @@ extern "C" int emc_iterate(emc_plan* p, float* d_model, float* d_weight, float s
   if ((rc = mark(3))) return rc;
   double* row_mass = p->red + kRedSlots;
   double* row_bound = row_mass + p->Rp;
-  mprep_kernel<<<R, 256, 0, ctx->stream>>>(p->L, p->PHI, p->lse, p->Ksum, R, N,
-                                            p->d.precision == EMC_PREC_FP32 ? p->Q : nullptr,
-                                            p->Np, p->T, row_mass, row_bound);
+  const bool tcm = p->d.precision == EMC_PREC_MIXED;
+  mprep_kernel<<<R, 256, 0, ctx->stream>>>(p->L, p->PHI, p->lse, p->Ksum, p->cnorm, R, N,
+                                            tcm ? nullptr : p->Q, tcm ? p->Qh : nullptr,
+                                            tcm ? p->Ql : nullptr, p->qscale, p->Np, p->T,
+                                            row_mass, row_bound);
   if ((rc = after_launch(ctx, "mprep_kernel"))) return rc;
   if ((rc = mark(4))) return rc;
   // M-step into zeroed accumulators
@@ -1118,6 +1161,17 @@ extern "C" int emc_iterate(emc_plan* p, float* d_model, float* d_weight, float s
     stats->reserved = 0;
   }
   return EMC_OK;
+}
+
+extern "C" int emc_plan_set_option(emc_plan* p, int option, int value) {
+  if (!p) return EMC_ERR_INVALID;
+  emc_ctx* ctx = p->ctx;
+  if (option == EMC_OPT_ESTEP_CLUSTER) {
+    EMC_REQUIRE(ctx, value == 1 || value == 2 || value == 4, "plan_set_option: cluster %d", value);
+    p->estep_cluster = value;
+    return EMC_OK;
+  }
+  return fail(ctx, EMC_ERR_INVALID, "plan_set_option: unknown option %d", option);
 }
 
 extern "C" int emc_plan_set_profiling(emc_plan* p, int on) {

@@ -59,6 +59,7 @@ struct emc_plan {
   float* Q = nullptr;      // [R][N] responsibility / scaling (FP32 M-step)
   __half* Qh = nullptr;    // [Rp][Np] hi (tensor-core M-step)
   __half* Ql = nullptr;    // [Rp][Np] lo
+  float* qscale = nullptr; // [Rp] 2^-e_r of the Q rows
   float2* part = nullptr;  // [n_rt][N] (max, sumexp) per rotation tile
   double* lse = nullptr;   // [N]
   float* T = nullptr;      // [Rp] rotation totals
@@ -73,6 +74,7 @@ struct emc_plan {
   cudaEvent_t ev[kPhases + 1] = {};
 
   void* tc = nullptr;  // tensor-core state (tensor maps, rotation operands)
+  int estep_cluster = 2;  // CTAs per cluster sharing rotation tiles (1, 2, 4)
 
   std::vector<void*> allocs;
   size_t bytes = 0;

@@ -149,7 +149,9 @@ __global__ void tc_rot_ops_kernel(const float* __restrict__ S, size_t n, __half*
   const size_t stride = (size_t)gridDim.x * blockDim.x;
   for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += stride) {
     const float s = S[e];
-    const bool mp = (double)s > 1e-10;
+    // (double)s > 1e-10 of the reference, as a float test: 1e-10f is the
+    // first float above 1e-10, so both agree for every float s
+    const bool mp = s >= 1e-10f;
     const bool m = s > 0.0f;
     const float ms = mp ? s * kMSScale : 0.0f;
     if (ms > 60000.0f) atomicOr(flags, 4);
@@ -196,6 +198,13 @@ struct TcEstepArgs {
   int* status;
 };
 
+// CL > 1: launched in clusters of CL CTAs that share one rotation tile and
+// hold CL consecutive pattern tiles.  Each CTA loads 128/CL rows of every
+// rotation-side tile and multicasts them to the whole cluster, so L2 serves
+// each rotation-side byte once per cluster instead of once per CTA; every
+// CTA's MMA completion is multicast to all empty barriers (arrival count
+// CL), so no stage is overwritten before the whole cluster has consumed it.
+template <int CL>
 __global__ void __launch_bounds__(es::THREADS, 1)
     tc_estep_kernel(const __grid_constant__ CUtensorMap mK, const __grid_constant__ CUtensorMap mK2h,
                     const __grid_constant__ CUtensorMap mK2l, const __grid_constant__ CUtensorMap mMp,
@@ -214,20 +223,23 @@ __global__ void __launch_bounds__(es::THREADS, 1)
   float* s_lw = s_scale + BN;
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  // grouped raster: GROUP rotation tiles share each pattern tile in turn
-  const int t = blockIdx.x;
-  const int per_group = GROUP * a.n_pt;
-  const int g = t / per_group, within = t % per_group;
+  // grouped raster over clusters: GROUP rotation tiles share each cluster of
+  // CL pattern tiles in turn
+  const int member = CL > 1 ? (int)ptx::cluster_ctarank() : 0;
+  const int cid = blockIdx.x / CL;
+  const int n_ptc = a.n_pt / CL;
+  const int per_group = GROUP * n_ptc;
+  const int g = cid / per_group, within = cid % per_group;
   const int rt0 = g * GROUP;
   const int gsz = min(GROUP, a.n_rt - rt0);
   const int rt = rt0 + within % gsz;
-  const int pt = within / gsz;
+  const int pt = (within / gsz) * CL + member;
   const int n0 = pt * BM, r0 = rt * BN;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
       ptx::mbar_init(&full[s], 1);
-      ptx::mbar_init(&empty[s], 1);
+      ptx::mbar_init(&empty[s], CL);
     }
     ptx::mbar_init(accum, 1);
     ptx::fence_mbar_init();
@@ -245,9 +257,12 @@ __global__ void __launch_bounds__(es::THREADS, 1)
   }
   ptx::tc_fence_before();
   __syncthreads();
+  if (CL > 1) ptx::cluster_sync();  // peers' barriers exist before any multicast
   ptx::tc_fence_after();
   const uint32_t tmem = *tmem_slot;
   const unsigned char* flags = a.k2lo_any + (size_t)pt * a.nkb;
+  constexpr uint16_t kAll = (uint16_t)((1u << CL) - 1);
+  constexpr int kRows = BN / CL;  // rotation rows each cluster member fetches
 
   if (warp == 0) {
     // ------------------------------------------------ TMA producer
@@ -265,8 +280,15 @@ __global__ void __launch_bounds__(es::THREADS, 1)
           if (j == 2 && !lo) continue;
           ptx::tma_load_2d(st + j * TILE_BYTES, amap[j], kb * BK, n0, &full[s]);
         }
-        for (int j = 0; j < NB; ++j)
-          ptx::tma_load_2d(st + (NA + j) * TILE_BYTES, bmap[j], kb * BK, r0, &full[s]);
+        for (int j = 0; j < NB; ++j) {
+          if (CL == 1) {
+            ptx::tma_load_2d(st + (NA + j) * TILE_BYTES, bmap[j], kb * BK, r0, &full[s]);
+          } else {
+            // rows member*kRows..+kRows-1 of the tile, to the same offset in every CTA
+            ptx::tma_load_2d_multicast(st + (NA + j) * TILE_BYTES + member * kRows * BK * 2,
+                                       bmap[j], kb * BK, r0 + member * kRows, &full[s], kAll);
+          }
+        }
       }
     }
   } else if (warp == 1) {
@@ -299,7 +321,10 @@ __global__ void __launch_bounds__(es::THREADS, 1)
           ptx::mma_f16(tmem + 384, aK2h, bHl, idesc, 1);
           if (lo) ptx::mma_f16(tmem + 384, aK2l, bHh, idesc, 1);
         }
-        ptx::mma_commit(&empty[s]);
+        if (CL == 1)
+          ptx::mma_commit(&empty[s]);
+        else
+          ptx::mma_commit_multicast(&empty[s], kAll);  // frees the stage in every CTA
       }
       ptx::mma_commit(accum);  // fires when every MMA above has completed
     }
@@ -361,6 +386,9 @@ __global__ void __launch_bounds__(es::THREADS, 1)
     ptx::tc_fence_after();
     ptx::tmem_dealloc(tmem, 512);
   }
+  // peers may still multicast MMA completions to this CTA's empty barriers
+  // until their last MMA retires: leave only together
+  if (CL > 1) ptx::cluster_sync();
 }
 
 // ------------------------------------------------------------ M-step -----
@@ -547,54 +575,11 @@ __global__ void __launch_bounds__(ms::THREADS, 1)
   }
 }
 
-// Q = P c_i / phi (phi holds c_i num/den, the M-step multiplies raw
-// counts) as FP16 hi + lo, each rotation row scaled by 2^e_r so that its
-// largest entry sits near 2^14: qscale_r = 2^-e_r.
-__global__ void __launch_bounds__(256) tc_qsplit_kernel(const float* __restrict__ P,
-                                                        const float* __restrict__ PHI,
-                                                        const float* __restrict__ cnorm, int R, int N,
-                                                        int Np, __half* __restrict__ Qh,
-                                                        __half* __restrict__ Ql,
-                                                        float* __restrict__ qscale) {
-  const int r = blockIdx.x;
-  float mx = 0.0f;
-  for (int i = threadIdx.x; i < N; i += blockDim.x) {
-    const size_t e = (size_t)r * N + i;
-    const float f = PHI[e];
-    const float q = f > 0.0f ? P[e] * __ldg(cnorm + i) / f : 0.0f;
-    mx = fmaxf(mx, q);
-  }
-  __shared__ float sm[256];
-  sm[threadIdx.x] = mx;
-  __syncthreads();
-  for (int o = 128; o > 0; o >>= 1) {
-    if (threadIdx.x < o) sm[threadIdx.x] = fmaxf(sm[threadIdx.x], sm[threadIdx.x + o]);
-    __syncthreads();
-  }
-  mx = sm[0];
-  int e = 0;
-  if (mx > 0.0f) e = 14 - ilogbf(mx) - 1;
-  e = max(-100, min(100, e));
-  const float up = ldexpf(1.0f, e);
-  for (int i = threadIdx.x; i < Np; i += blockDim.x) {
-    float q = 0.0f;
-    if (i < N) {
-      const size_t o = (size_t)r * N + i;
-      const float f = PHI[o];
-      q = f > 0.0f ? P[o] * __ldg(cnorm + i) / f * up : 0.0f;
-    }
-    const __half hi = __float2half_rn(q);
-    Qh[(size_t)r * Np + i] = hi;
-    Ql[(size_t)r * Np + i] = __float2half_rn(q - __half2float(hi));
-  }
-  if (threadIdx.x == 0) qscale[r] = ldexpf(1.0f, -e);
-}
-
 // ------------------------------------------------------------ host -------
 struct TcState {
-  CUtensorMap mK, mK2h, mK2l, mMp, mMS, mGh, mGl, mHh, mHl, mQh, mQl, mKt;
+  CUtensorMap mK, mK2h, mK2l, mQh, mQl, mKt;
+  CUtensorMap rot[3][6];  // rotation-side maps, box rows 128 / {1, 2, 4}
   __half *Mp, *MSh, *Gh, *Gl, *Hh, *Hl;
-  float* qscale;
   int* status;
 };
 
@@ -624,7 +609,7 @@ int tc_bind(emc_plan* p) {
       if (!rc) rc = plan_alloc(p, (void**)pp, rk * 2);
     if (!rc) rc = plan_alloc(p, (void**)&p->Qh, (size_t)Rp * Np * 2);
     if (!rc) rc = plan_alloc(p, (void**)&p->Ql, (size_t)Rp * Np * 2);
-    if (!rc) rc = plan_alloc(p, (void**)&st->qscale, (size_t)Rp * 4);
+    if (!rc) rc = plan_alloc(p, (void**)&p->qscale, (size_t)Rp * 4);
     if (!rc) rc = plan_alloc(p, (void**)&st->status, 64);
     if (rc) return rc;
     EMC_CUDA(ctx, cudaMemsetAsync(p->Qh, 0, (size_t)Rp * Np * 2, ctx->stream));
@@ -634,14 +619,18 @@ int tc_bind(emc_plan* p) {
     if (!rc) rc = make_map(ctx, &st->mK2h, p->K2hi, Np, Kp, 128, 32);
     if (!rc) rc = make_map(ctx, &st->mK2l, p->K2lo, Np, Kp, 128, 32);
     const __half* ro[6] = {st->Mp, st->MSh, st->Gh, st->Gl, st->Hh, st->Hl};
-    CUtensorMap* rm[6] = {&st->mMp, &st->mMS, &st->mGh, &st->mGl, &st->mHh, &st->mHl};
-    for (int j = 0; j < 6 && !rc; ++j) rc = make_map(ctx, rm[j], ro[j], Rp, Kp, 128, 32);
+    for (int c = 0; c < 3; ++c)
+      for (int j = 0; j < 6 && !rc; ++j) rc = make_map(ctx, &st->rot[c][j], ro[j], Rp, Kp, 128 >> c, 32);
     if (!rc) rc = make_map(ctx, &st->mQh, p->Qh, Rp, Np, 128, 64);
     if (!rc) rc = make_map(ctx, &st->mQl, p->Ql, Rp, Np, 128, 64);
     if (!rc) rc = make_map(ctx, &st->mKt, p->KhT, Kp, Np, 256, 64);
     if (rc) return rc;
-    EMC_CUDA(ctx, cudaFuncSetAttribute(tc_estep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       es::SMEM_BYTES));
+    EMC_CUDA(ctx, cudaFuncSetAttribute(tc_estep_kernel<1>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, es::SMEM_BYTES));
+    EMC_CUDA(ctx, cudaFuncSetAttribute(tc_estep_kernel<2>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, es::SMEM_BYTES));
+    EMC_CUDA(ctx, cudaFuncSetAttribute(tc_estep_kernel<4>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, es::SMEM_BYTES));
     EMC_CUDA(ctx, cudaFuncSetAttribute(tc_mstep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        ms::SMEM_BYTES));
   }
@@ -697,21 +686,39 @@ int tc_estep(emc_plan* p, float sigma) {
   a.part = p->part;
   a.bad = p->flags + 4;
   a.status = st->status;
-  const int tiles = a.n_pt * a.n_rt;
-  tc_estep_kernel<<<tiles, es::THREADS, es::SMEM_BYTES, ctx->stream>>>(
-      st->mK, st->mK2h, st->mK2l, st->mMp, st->mMS, st->mGh, st->mGl, st->mHh, st->mHl, a);
-  if ((rc = after_launch(ctx, "tc_estep_kernel"))) return rc;
-  return EMC_OK;
+  const int cl = p->estep_cluster;
+  const int c = cl == 4 ? 2 : cl == 2 ? 1 : 0;
+  const CUtensorMap* rm = st->rot[c];
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(a.n_pt * a.n_rt);
+  cfg.blockDim = dim3(es::THREADS);
+  cfg.dynamicSmemBytes = es::SMEM_BYTES;
+  cfg.stream = ctx->stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = cl;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cudaError_t e;
+  if (cl == 4)
+    e = cudaLaunchKernelEx(&cfg, tc_estep_kernel<4>, st->mK, st->mK2h, st->mK2l, rm[0], rm[1],
+                           rm[2], rm[3], rm[4], rm[5], a);
+  else if (cl == 2)
+    e = cudaLaunchKernelEx(&cfg, tc_estep_kernel<2>, st->mK, st->mK2h, st->mK2l, rm[0], rm[1],
+                           rm[2], rm[3], rm[4], rm[5], a);
+  else
+    e = cudaLaunchKernelEx(&cfg, tc_estep_kernel<1>, st->mK, st->mK2h, st->mK2l, rm[0], rm[1],
+                           rm[2], rm[3], rm[4], rm[5], a);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "tc_estep_kernel launch");
+  return after_launch(ctx, "tc_estep_kernel");
 }
 
 int tc_mstep(emc_plan* p, float* model, float* weight) {
   emc_ctx* ctx = p->ctx;
   TcState* st = state(p);
   int rc;
-  tc_qsplit_kernel<<<p->d.n_rot, 256, 0, ctx->stream>>>(p->L, p->PHI, p->cnorm, p->d.n_rot,
-                                                        p->d.n_images, p->Np, p->Qh, p->Ql,
-                                                        st->qscale);
-  if ((rc = after_launch(ctx, "tc_qsplit_kernel"))) return rc;
   TcMstepArgs a;
   a.R = p->d.n_rot;
   a.Kp = p->Kp;
@@ -721,7 +728,7 @@ int tc_mstep(emc_plan* p, float* model, float* weight) {
   a.n_rt = p->Rp / ms::BM;
   a.nkb = p->Np / ms::BK;
   a.T = p->T;
-  a.qscale = st->qscale;
+  a.qscale = p->qscale;
   a.rot = p->rot;
   a.cx = p->cx;
   a.cy = p->cy;

@@ -199,6 +199,49 @@ def make_problem(cfg: Config, device: str | None = None, coords=None, rotations=
     return Problem(cfg, true.reshape(-1), init, images, mask, x, y, z, quats, weights, tq, scales)
 
 
+def write_problem(prob: Problem, directory, iterations=1, extra=""):
+    """Writes the `emc` driver's inputs: images.bin (float32 [N][s*s]),
+    mask.bin (int32 [s*s]), model.bin (float32 [s^3], read with model_input 2)
+    and an emc.conf that points at them.  Returns the config path."""
+    import os
+    d = os.path.abspath(str(directory))
+    os.makedirs(d, exist_ok=True)
+    c = prob.cfg
+    np.ascontiguousarray(prob.images, np.float32).tofile(os.path.join(d, "images.bin"))
+    np.ascontiguousarray(prob.mask, np.int32).tofile(os.path.join(d, "mask.bin"))
+    np.ascontiguousarray(prob.init_model, np.float32).tofile(os.path.join(d, "model.bin"))
+    conf = os.path.join(d, "emc.conf")
+    with open(conf, "w") as f:
+        f.write(f"""# synthetic problem {c.name}
+model_side = {c.side};
+read_stride = 1;
+wavelength = {WAVELENGTH!r};
+pixel_size = {PIXEL_SIZE!r};
+detector_size = {c.side};
+detector_distance = {DISTANCE!r};
+rotations_n = {c.rot_n};
+sigma_start = {SIGMA_START};
+sigma_final = {SIGMA_FINAL};
+sigma_half_life = {SIGMA_HALF_LIFE};
+diff_type = "poisson";
+slice_chunk = 5000;
+N_images = {c.n_images};
+max_iterations = {iterations};
+image_prefix = "{d}/";
+mask_file = "{d}/mask.bin";
+normalize_images = false;
+known_intensity = false;
+model_input = 2;
+model_file = "{d}/model.bin";
+isOutput = 1;
+output_loop = 0;
+output_period = 1;
+isDebug = 1;
+{extra}
+""")
+    return conf
+
+
 def _render_torch(model, tq, pts, mask, scales, cfg, device):
     """GPU rendering of the Poisson patterns (torch; the generator is seeded)."""
     import torch

@@ -262,6 +262,11 @@ int emc_plan_bind(emc_plan* plan, const float* d_images, const int* d_mask, cons
  * stats (host, may be NULL) is filled after a synchronise. */
 int emc_iterate(emc_plan* plan, float* d_model, float* d_weight, float sigma,
                 emc_iter_stats* stats);
+/* Tuning of the tensor-core kernels (the autotuner's knobs).
+ * EMC_OPT_ESTEP_CLUSTER: CTAs per thread-block cluster of the E-step (1, 2,
+ * 4); the cluster shares rotation-side tiles through TMA multicast. */
+#define EMC_OPT_ESTEP_CLUSTER 1
+int emc_plan_set_option(emc_plan* plan, int option, int value);
 /* Instrumentation: with profiling on, emc_iterate records CUDA events on the
  * context stream between its phases; emc_plan_phase_ms (after the iteration
  * completes) returns the durations of expand, E-step (scaling + likelihood),

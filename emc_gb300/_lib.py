@@ -85,6 +85,7 @@ SIGNATURES: dict[str, tuple] = {
     "emc_calculate_responsabilities": (I, [P, P, P, P, F, P, P, P, I, I, I, I, I]),
     "emc_max_vector": (I, [P, P, I, I, P]),
     "emc_respons_max_expf": (I, [P, P, P, I, I, P]),
+    "emc_respons_max_expf_noalloc": (I, [P, P, I, I, P, P]),
     "emc_norm_respons_sumexpf": (I, [P, P, P, P, I, I]),
     "emc_log_sum_max": (I, [P, P, P, P, I]),
     "emc_update_slices": (I, [P, P, P, P, P, P, P, I, I, I, I, I, P, P, P, P, P, P]),

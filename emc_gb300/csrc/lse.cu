@@ -17,6 +17,7 @@
 // use a different order than the reference's 512-way tree and so agree to
 // float rounding.
 #include <algorithm>
+#include <mutex>
 
 #include "common.cuh"
 
@@ -169,3 +170,61 @@ extern "C" int emc_log_sum_max(emc_ctx* ctx, const float* d_sum, const float* d_
   return emc::after_launch(ctx, "log_sum_max_kernel");
 }
 
+// ---- allocation-free variant of emc_respons_max_expf ---------------------
+// For callers that must not allocate device memory at the time of the call:
+// code running inside CUDA stream capture, callbacks and real-time loops
+// where cudaMalloc would synchronise the device or is forbidden, and hosts
+// that hand the library a fixed memory budget.  The per-range partial sums
+// live in one file-scope device array of EMC_NOALLOC_PARTIALS floats (4 MiB),
+// which every GPU that loads this library keeps until the process exits.
+// Host code never dereferences the array's name (on the host it is only a
+// stand-in symbol): its device address is looked up with
+// cudaGetSymbolAddress on the first call made on each device, with that
+// device current, and cached; that first call therefore does the set-up and
+// should come before any stream capture.  No cudaMalloc, cudaFree or
+// allocating library routine is called.  Every call on a device shares the
+// array and each call overwrites every slot it reads, so nothing has to be
+// cleared; calls whose kernels overlap on the GPU (e.g. on two streams) race
+// on the array and must be serialised by the caller.
+static __device__ __align__(256) float g_noalloc_partials[EMC_NOALLOC_PARTIALS];
+
+static int noalloc_partials(float** out) {
+  static std::mutex mu;
+  static float* addr[64] = {};
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return EMC_ERR_CUDA;
+  std::lock_guard<std::mutex> lock(mu);
+  if (!addr[dev]) {
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_noalloc_partials) != cudaSuccess || !p) return EMC_ERR_CUDA;
+    addr[dev] = (float*)p;
+  }
+  *out = addr[dev];
+  return EMC_OK;
+}
+
+extern "C" int emc_respons_max_expf_noalloc(const float* d_respons, const float* d_max,
+                                            int N_images, int n_slices, float* d_sum,
+                                            void* cuda_stream) {
+  if (!d_respons || !d_max || !d_sum || N_images < 0 || n_slices < 0) return EMC_ERR_INVALID;
+  if (N_images > EMC_NOALLOC_PARTIALS) return EMC_ERR_INVALID;  // not even one range fits
+  if (N_images == 0) return EMC_OK;
+  cudaStream_t stream = (cudaStream_t)cuda_stream;
+  float* part = nullptr;
+  const int max_ranges = std::min(EMC_NOALLOC_PARTIALS / N_images, 65535);
+  int rc = 64, nb = 0;
+  if (n_slices > 0) {
+    rc = std::max(64, (n_slices + max_ranges - 1) / max_ranges);
+    nb = (n_slices + rc - 1) / rc;
+    const int e = noalloc_partials(&part);
+    if (e) return e;
+  }
+  const int gx = emc::ceil_div(N_images, emc::kLseThreads);
+  if (nb > 0) {
+    emc::sumexp_partial_kernel<<<dim3(gx, nb), emc::kLseThreads, 0, stream>>>(
+        d_respons, d_max, N_images, n_slices, rc, part);
+    if (cudaGetLastError() != cudaSuccess) return EMC_ERR_CUDA;
+  }
+  emc::sum_final_kernel<<<gx, emc::kLseThreads, 0, stream>>>(part, N_images, nb, d_sum);
+  return cudaGetLastError() == cudaSuccess ? EMC_OK : EMC_ERR_CUDA;
+}

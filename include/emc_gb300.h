@@ -163,6 +163,21 @@ int emc_respons_max_expf(emc_ctx* ctx, const float* d_respons, const float* d_ma
 int emc_norm_respons_sumexpf(emc_ctx* ctx, float* d_respons, const float* d_sum,
                              const float* d_max, int N_images, int n_slices);
 
+/* Allocation-free form of emc_respons_max_expf, for callers that cannot call
+ * cudaMalloc when they run it (inside stream capture, in callbacks, under a
+ * fixed device-memory budget).  No counterpart in the reference: its
+ * cuda_respons_max_expf allocates an R x N temporary on every call.
+ * Needs no context: work is queued on `cuda_stream` (NULL = legacy default
+ * stream).  Scratch is a file-scope device array of EMC_NOALLOC_PARTIALS
+ * floats (4 MiB per GPU that loads the library, held until exit), so
+ * N_images may not exceed EMC_NOALLOC_PARTIALS (EMC_ERR_INVALID otherwise).
+ * The first call on each device looks up the array's device address
+ * (cudaGetSymbolAddress, no allocation) and should come before any stream
+ * capture.  Calls that overlap on the GPU share the array and race. */
+#define EMC_NOALLOC_PARTIALS (1 << 20)
+int emc_respons_max_expf_noalloc(const float* d_respons, const float* d_max, int N_images,
+                                 int n_slices, float* d_sum, void* cuda_stream);
+
 /* Convenience for the host step between the two calls above
  * (emc_helper.cpp:579-587 log_vector + sum_vectors, float):
  * lse[i] = logf(sum[i]) + max[i], on the device. */

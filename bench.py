@@ -361,8 +361,8 @@ def finish(args, prob, plan, ctx, ws, rank, precision, value, ms_step, st, plain
     flops = 8.0 * p_eff * pairs  # 4 GEMM-equivalents (num, den, B, C) x 2 FLOP
     est = statistics.mean(estep_ms)
     achieved = flops / (est / 1e3) / 1e12
-    kernel = "estep_tc" if precision == "mixed" else "estep_fp32"
-    traffic = profile_traffic(kernel)
+    kernel = "tc_estep_kernel" if precision == "mixed" else "estep_fp32_kernel"
+    traffic = profile_traffic(f"{kernel}_{prob.cfg.name}")
     roofline = {"bound": "tensor", "kernel": kernel, "achieved": achieved,
                 "peak": peaks["bf16"], "unit": "TFLOP/s", "frac": achieved / peaks["bf16"],
                 "peak_source": f"bf16_tflops of {peaks['source']} peaks",

@@ -74,7 +74,7 @@ struct emc_plan {
   cudaEvent_t ev[kPhases + 1] = {};
 
   void* tc = nullptr;  // tensor-core state (tensor maps, rotation operands)
-  int estep_cluster = 2;  // CTAs per cluster sharing rotation tiles (1, 2, 4)
+  int estep_cluster = 1;  // CTAs per cluster sharing rotation tiles (1, 2, 4)
 
   std::vector<void*> allocs;
   size_t bytes = 0;

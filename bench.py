@@ -49,6 +49,8 @@ def parse():
     ap.add_argument("--config", default="mid")
     ap.add_argument("--precision", choices=["auto", "mixed", "fp32"], default="auto")
     ap.add_argument("--insert", choices=["atomic", "deterministic"], default="atomic")
+    ap.add_argument("--mstep-qlo", type=int, choices=[0, 1], default=1,
+                    help="tensor M-step: responsibility x scaling as FP16 hi+lo (1) or hi (0)")
     ap.add_argument("--plain-steps", type=int, default=2)
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
@@ -241,6 +243,7 @@ def run_ours(args):
 
     def new_plan(prec):
         p = E.Plan(ctx, s, N, R, precision=prec, insert_mode=insert)
+        p.set_option(E.Plan.OPT_MSTEP_QLO, args.mstep_qlo)
         p.bind(images, mask, x, y, z, rot, w)
         return p
 
@@ -384,7 +387,8 @@ def finish(args, prob, plan, ctx, ws, rank, precision, value, ms_step, st, plain
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32" if precision == "fp32" else "f16/f32",
             "data": "synthetic (seeded; shapes of the mid-size configuration)",
-            "config": workload_desc(prob, precision, args.insert),
+            "config": dict(workload_desc(prob, precision, args.insert),
+                           mstep_q="fp16 hi+lo" if args.mstep_qlo else "fp16 hi"),
             "iter_per_s": ws * 1e3 / ms_step,
             "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "plain_fp32": plain,
             "speedup_vs_plain_fp32": (plain["ms_per_step"] / ms_step) if plain else None,

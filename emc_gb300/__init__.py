@@ -278,6 +278,7 @@ class Plan:
 
     PHASES = ("expand", "estep", "lse", "mprep", "mstep", "finish")
     OPT_ESTEP_CLUSTER = 1
+    OPT_MSTEP_QLO = 2
 
     def set_option(self, option: int, value: int):
         self.ctx._check(self._lib.emc_plan_set_option(self._h, option, value), "plan_set_option")

@@ -640,6 +640,7 @@ struct InsertCtx {
   float* weight;
   unsigned long long* fix_m;
   unsigned long long* fix_w;
+  float2* acc2;          // interleaved (model, weight) sums: one 8-byte atomic per point
   const double* bounds;  // {model, weight} inserted-mass bounds (deterministic mode)
   int side;
   int interp;
@@ -657,8 +658,7 @@ __device__ __forceinline__ void add_voxel(const InsertCtx& c, size_t v, float va
     atomicAdd(c.fix_m + v, (unsigned long long)__double2ll_rn((double)val * fixed_scale(c.bounds[0])));
     atomicAdd(c.fix_w + v, (unsigned long long)__double2ll_rn((double)w * fixed_scale(c.bounds[1])));
   } else {
-    atomicAdd(c.model + v, val);
-    atomicAdd(c.weight + v, w);
+    atomicAdd(c.acc2 + v, make_float2(val, w));
   }
 }
 
@@ -812,16 +812,29 @@ __global__ void insert_bounds_kernel(const double* __restrict__ row_mass,
   }
 }
 
-__global__ void fixed_to_model_kernel(const unsigned long long* __restrict__ fm,
-                                      const unsigned long long* __restrict__ fw,
-                                      const double* __restrict__ bounds, float* __restrict__ model,
-                                      float* __restrict__ weight, long long n) {
-  const double inv_m = 1.0 / fixed_scale(bounds[0]);
-  const double inv_w = 1.0 / fixed_scale(bounds[1]);
+// Inserted sums -> weight and model / weight (-1 where the weight is 0,
+// emc_cuda.cu:758-768), from the fixed-point (deterministic) or the
+// interleaved float accumulators.
+__global__ void finish_insert_kernel(const unsigned long long* __restrict__ fm,
+                                     const unsigned long long* __restrict__ fw,
+                                     const double* __restrict__ bounds,
+                                     const float2* __restrict__ acc2, float* __restrict__ model,
+                                     float* __restrict__ weight, long long n) {
+  const double inv_m = fm ? 1.0 / fixed_scale(bounds[0]) : 0.0;
+  const double inv_w = fm ? 1.0 / fixed_scale(bounds[1]) : 0.0;
   const long long stride = (long long)gridDim.x * blockDim.x;
   for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += stride) {
-    model[v] = (float)((double)(long long)fm[v] * inv_m);
-    weight[v] = (float)((double)(long long)fw[v] * inv_w);
+    float m, w;
+    if (fm) {
+      m = (float)((double)(long long)fm[v] * inv_m);
+      w = (float)((double)(long long)fw[v] * inv_w);
+    } else {
+      const float2 a = acc2[v];
+      m = a.x;
+      w = a.y;
+    }
+    weight[v] = w;
+    model[v] = w > 0.0f ? __fdiv_rn(m, w) : -1.0f;
   }
 }
 
@@ -875,6 +888,7 @@ extern "C" int emc_plan_create(emc_ctx* ctx, const emc_plan_desc* desc, emc_plan
     rc = alloc_n(p, &p->fix_m, n3);
     if (!rc) rc = alloc_n(p, &p->fix_w, n3);
   }
+  if (!rc && d.insert_mode == EMC_INSERT_ATOMIC) rc = alloc_n(p, &p->acc2, n3);
   if (rc) {
     emc_plan_destroy(p);
     return rc;
@@ -1031,6 +1045,7 @@ static InsertCtx make_insert_ctx(emc_plan* p, float* model, float* weight) {
   c.weight = weight;
   c.fix_m = p->fix_m;
   c.fix_w = p->fix_w;
+  c.acc2 = p->acc2;
   c.bounds = p->red + kRedBoundM;
   c.side = p->d.side;
   c.interp = p->d.interp;
@@ -1112,8 +1127,7 @@ extern "C" int emc_iterate(emc_plan* p, float* d_model, float* d_weight, float s
     EMC_CUDA(ctx, cudaMemsetAsync(p->fix_m, 0, sizeof(unsigned long long) * n3, ctx->stream));
     EMC_CUDA(ctx, cudaMemsetAsync(p->fix_w, 0, sizeof(unsigned long long) * n3, ctx->stream));
   } else {
-    EMC_CUDA(ctx, cudaMemsetAsync(d_model, 0, sizeof(float) * n3, ctx->stream));
-    EMC_CUDA(ctx, cudaMemsetAsync(d_weight, 0, sizeof(float) * n3, ctx->stream));
+    EMC_CUDA(ctx, cudaMemsetAsync(p->acc2, 0, sizeof(float2) * n3, ctx->stream));
   }
   InsertCtx ins = make_insert_ctx(p, d_model, d_weight);
   if (p->d.precision == EMC_PREC_MIXED)
@@ -1121,15 +1135,14 @@ extern "C" int emc_iterate(emc_plan* p, float* d_model, float* d_weight, float s
   else
     rc = plan_mstep_fp32(p, d_model, d_weight, ins);
   if (rc) return rc;
-  if (det) {
+  {
     const int nb = (int)std::min<long long>(ceil_div(n3, 256), (long long)ctx->sm_count * 8);
-    fixed_to_model_kernel<<<nb, 256, 0, ctx->stream>>>(p->fix_m, p->fix_w, ins.bounds, d_model,
-                                                        d_weight, n3);
-    if ((rc = after_launch(ctx, "fixed_to_model_kernel"))) return rc;
+    finish_insert_kernel<<<nb, 256, 0, ctx->stream>>>(det ? p->fix_m : nullptr, p->fix_w, ins.bounds,
+                                                       p->acc2, d_model, d_weight, n3);
+    if ((rc = after_launch(ctx, "finish_insert_kernel"))) return rc;
   }
   if ((rc = mark(5))) return rc;
-  // divide, normalise, blur
-  if ((rc = launch_divide_by_weight(ctx, d_model, d_weight, n3))) return rc;
+  // normalise, blur
   double* mean_stats = p->red + kRedMean;
   // launch_positive_mean writes {sum, count} then its partials after them;
   // kRedMean + 2 + 2*1024 fits in the reduction buffer tail.
@@ -1169,6 +1182,11 @@ extern "C" int emc_plan_set_option(emc_plan* p, int option, int value) {
   if (option == EMC_OPT_ESTEP_CLUSTER) {
     EMC_REQUIRE(ctx, value == 1 || value == 2 || value == 4, "plan_set_option: cluster %d", value);
     p->estep_cluster = value;
+    return EMC_OK;
+  }
+  if (option == EMC_OPT_MSTEP_QLO) {
+    EMC_REQUIRE(ctx, value == 0 || value == 1, "plan_set_option: q_lo %d", value);
+    p->mstep_q_lo = value;
     return EMC_OK;
   }
   return fail(ctx, EMC_ERR_INVALID, "plan_set_option: unknown option %d", option);

@@ -66,6 +66,7 @@ struct emc_plan {
   double* red = nullptr;   // reduction scratch (small)
   unsigned long long* fix_m = nullptr;  // [s^3] fixed-point model (deterministic insert)
   unsigned long long* fix_w = nullptr;
+  float2* acc2 = nullptr;  // [s^3] interleaved (model, weight) sums (float atomics)
   int* flags = nullptr;    // device status words
 
   // per-phase CUDA events on the context stream (emc_plan_set_profiling)
@@ -75,6 +76,7 @@ struct emc_plan {
 
   void* tc = nullptr;  // tensor-core state (tensor maps, rotation operands)
   int estep_cluster = 1;  // CTAs per cluster sharing rotation tiles (1, 2, 4)
+  int mstep_q_lo = 1;     // tensor M-step: Q as FP16 hi + lo (1) or hi only (0)
 
   std::vector<void*> allocs;
   size_t bytes = 0;

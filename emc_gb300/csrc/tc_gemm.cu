@@ -416,7 +416,9 @@ struct TcMstepArgs {
   float* weight;
   unsigned long long* fix_m;
   unsigned long long* fix_w;
+  float2* acc2;
   const double* bounds;
+  int q_lo;  // 1: Q hi + lo, 0: Q hi only
   int* status;
 };
 
@@ -429,8 +431,7 @@ __device__ __forceinline__ void tc_add(const TcMstepArgs& a, size_t v, float val
     atomicAdd(a.fix_m + v, (unsigned long long)__double2ll_rn((double)val * tc_fixed_scale(a.bounds[0])));
     atomicAdd(a.fix_w + v, (unsigned long long)__double2ll_rn((double)w * tc_fixed_scale(a.bounds[1])));
   } else {
-    atomicAdd(a.model + v, val);
-    atomicAdd(a.weight + v, w);
+    atomicAdd(a.acc2 + v, make_float2(val, w));  // model and weight in one 8-byte atomic
   }
 }
 
@@ -511,10 +512,10 @@ __global__ void __launch_bounds__(ms::THREADS, 1)
         const int s = kb % STAGES;
         const uint32_t ph = (kb / STAGES) & 1;
         if (!ptx::mbar_wait(&empty[s], ph ^ 1, a.status, 4)) break;
-        ptx::mbar_arrive_expect_tx(&full[s], STAGE_BYTES);
+        ptx::mbar_arrive_expect_tx(&full[s], STAGE_BYTES - (a.q_lo ? 0 : A_BYTES));
         unsigned char* st = smem + s * STAGE_BYTES;
         ptx::tma_load_2d(st, &mQh, kb * BK, r0, &full[s]);
-        ptx::tma_load_2d(st + A_BYTES, &mQl, kb * BK, r0, &full[s]);
+        if (a.q_lo) ptx::tma_load_2d(st + A_BYTES, &mQl, kb * BK, r0, &full[s]);
         ptx::tma_load_2d(st + 2 * A_BYTES, &mKt, kb * BK, q0, &full[s]);
       }
     }
@@ -533,7 +534,7 @@ __global__ void __launch_bounds__(ms::THREADS, 1)
           const uint64_t dQl = ptx::smem_desc(base + A_BYTES + ks * 32, 1024, 2);
           const uint64_t dK = ptx::smem_desc(base + 2 * A_BYTES + ks * 32, 1024, 2);
           ptx::mma_f16(tmem, dQh, dK, idesc, (kb | ks) ? 1u : 0u);
-          ptx::mma_f16(tmem, dQl, dK, idesc, 1u);
+          if (a.q_lo) ptx::mma_f16(tmem, dQl, dK, idesc, 1u);
         }
         ptx::mma_commit(&empty[s]);
       }
@@ -740,6 +741,8 @@ int tc_mstep(emc_plan* p, float* model, float* weight) {
   a.weight = weight;
   a.fix_m = p->fix_m;
   a.fix_w = p->fix_w;
+  a.acc2 = p->acc2;
+  a.q_lo = p->mstep_q_lo;
   a.bounds = p->red + kRedBoundM;
   a.status = st->status;
   const int tiles = a.n_qt * a.n_rt;

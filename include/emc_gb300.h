@@ -281,6 +281,10 @@ int emc_iterate(emc_plan* plan, float* d_model, float* d_weight, float sigma,
  * EMC_OPT_ESTEP_CLUSTER: CTAs per thread-block cluster of the E-step (1, 2,
  * 4); the cluster shares rotation-side tiles through TMA multicast. */
 #define EMC_OPT_ESTEP_CLUSTER 1
+/* EMC_OPT_MSTEP_QLO: 1 (default) multiplies responsibility/scaling as FP16
+ * hi + lo, 0 as FP16 hi only (half the M-step MMAs, ~2^-12 relative
+ * rounding per term). */
+#define EMC_OPT_MSTEP_QLO 2
 int emc_plan_set_option(emc_plan* plan, int option, int value);
 /* Instrumentation: with profiling on, emc_iterate records CUDA events on the
  * context stream between its phases; emc_plan_phase_ms (after the iteration

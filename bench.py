@@ -51,6 +51,13 @@ def parse():
     ap.add_argument("--insert", choices=["atomic", "deterministic"], default="atomic")
     ap.add_argument("--mstep-qlo", type=int, choices=[0, 1], default=1,
                     help="tensor M-step: responsibility x scaling as FP16 hi+lo (1) or hi (0)")
+    ap.add_argument("--diff", choices=["poisson", "true_poisson"], default="poisson",
+                    help="likelihood: the reference's poisson (weighted least squares) or "
+                         "the counts x log-slice Poisson likelihood")
+    ap.add_argument("--mstep-aggregate", type=int, choices=[0, 1], default=0,
+                    help="tensor M-step: warp-aggregated atomics for nearest insertion")
+    ap.add_argument("--estep-ghlo", type=int, choices=[0, 1], default=1,
+                    help="tensor E-step: rotation-side factors as FP16 hi+lo (1) or hi (0)")
     ap.add_argument("--plain-steps", type=int, default=2)
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
@@ -185,7 +192,7 @@ def workload_desc(prob, precision, insert):
                         f"(~{c.photons:g} photons, scale U{c.scale}, beamstop {c.beamstop} px), "
                         f"{prob.quats.shape[0]} rotations (n={c.rot_n}), one full EMC iteration",
             "side": c.side, "n_images": c.n_images, "n_rot": int(prob.quats.shape[0]),
-            "p_eff": int(prob.mask.sum()), "diff": "poisson (reference)", "interp": "nearest",
+            "p_eff": int(prob.mask.sum()), "interp": "nearest",
             "precision": precision, "insert": insert,
             "l2": "inputs larger than L2 (patterns 1.3 GB, responsibilities 2 GB per step)"}
 
@@ -242,8 +249,11 @@ def run_ours(args):
     insert = E.INSERT_DETERMINISTIC if args.insert == "deterministic" else E.INSERT_ATOMIC
 
     def new_plan(prec):
-        p = E.Plan(ctx, s, N, R, precision=prec, insert_mode=insert)
+        diff = E.DIFF_TRUE_POISSON if args.diff == "true_poisson" else E.DIFF_POISSON
+        p = E.Plan(ctx, s, N, R, diff=diff, precision=prec, insert_mode=insert)
         p.set_option(E.Plan.OPT_MSTEP_QLO, args.mstep_qlo)
+        p.set_option(E.Plan.OPT_ESTEP_GHLO, args.estep_ghlo)
+        p.set_option(E.Plan.OPT_MSTEP_AGGREGATE, args.mstep_aggregate)
         p.bind(images, mask, x, y, z, rot, w)
         return p
 
@@ -361,10 +371,14 @@ def finish(args, prob, plan, ctx, ws, rank, precision, value, ms_step, st, plain
     # ---- roofline of the dominant kernel (E-step)
     peaks = load_peaks()
     p_eff = int(prob.mask.sum())
-    flops = 8.0 * p_eff * pairs  # 4 GEMM-equivalents (num, den, B, C) x 2 FLOP
+    if args.diff == "poisson":
+        flops = 8.0 * p_eff * pairs  # 4 GEMM-equivalents (num, den, B, C) x 2 FLOP
+        kernel = "tc_estep_kernel" if precision == "mixed" else "estep_fp32_kernel"
+    else:
+        flops = 2.0 * p_eff * pairs  # one GEMM-equivalent (counts x log slice) x 2 FLOP
+        kernel = "tc_estep_pois_kernel" if precision == "mixed" else "estep_pois_fp32_kernel"
     est = statistics.mean(estep_ms)
     achieved = flops / (est / 1e3) / 1e12
-    kernel = "tc_estep_kernel" if precision == "mixed" else "estep_fp32_kernel"
     traffic = profile_traffic(f"{kernel}_{prob.cfg.name}")
     roofline = {"bound": "tensor", "kernel": kernel, "achieved": achieved,
                 "peak": peaks["bf16"], "unit": "TFLOP/s", "frac": achieved / peaks["bf16"],
@@ -388,7 +402,11 @@ def finish(args, prob, plan, ctx, ws, rank, precision, value, ms_step, st, plain
             "scaling": "weak", "vs_baseline": None, "dtype": "f32" if precision == "fp32" else "f16/f32",
             "data": "synthetic (seeded; shapes of the mid-size configuration)",
             "config": dict(workload_desc(prob, precision, args.insert),
-                           mstep_q="fp16 hi+lo" if args.mstep_qlo else "fp16 hi"),
+                           diff="poisson (reference)" if args.diff == "poisson"
+                           else "true poisson (counts x log slice)",
+                           mstep_q="fp16 hi+lo" if args.mstep_qlo else "fp16 hi",
+                           estep_gh="fp16 hi+lo" if args.estep_ghlo else "fp16 hi",
+                           mstep_atomics="warp-aggregated" if args.mstep_aggregate else "per pair"),
             "iter_per_s": ws * 1e3 / ms_step,
             "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "plain_fp32": plain,
             "speedup_vs_plain_fp32": (plain["ms_per_step"] / ms_step) if plain else None,

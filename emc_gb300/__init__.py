@@ -277,8 +277,9 @@ class Plan:
         return st if stats else None
 
     PHASES = ("expand", "estep", "lse", "mprep", "mstep", "finish")
-    OPT_ESTEP_CLUSTER = 1
+    OPT_ESTEP_GHLO = 3
     OPT_MSTEP_QLO = 2
+    OPT_MSTEP_AGGREGATE = 4
 
     def set_option(self, option: int, value: int):
         self.ctx._check(self._lib.emc_plan_set_option(self._h, option, value), "plan_set_option")

@@ -865,7 +865,7 @@ extern "C" int emc_plan_create(emc_ctx* ctx, const emc_plan_desc* desc, emc_plan
   p->ctx = ctx;
   p->d = d;
   p->n2 = d.side * d.side;
-  p->Np = ceil_div(d.n_images, 512) * 512;  // whole clusters of up to 4 pattern tiles
+  p->Np = ceil_div(d.n_images, 128) * 128;  // whole 128-pattern tiles (and 64-pattern k-blocks)
   p->Rp = ceil_div(d.n_rot, 128) * 128;
   p->n_rt = ceil_div(d.n_rot, EMC_RT);
   const size_t RN = (size_t)d.n_rot * d.n_images;
@@ -1179,9 +1179,14 @@ extern "C" int emc_iterate(emc_plan* p, float* d_model, float* d_weight, float s
 extern "C" int emc_plan_set_option(emc_plan* p, int option, int value) {
   if (!p) return EMC_ERR_INVALID;
   emc_ctx* ctx = p->ctx;
-  if (option == EMC_OPT_ESTEP_CLUSTER) {
-    EMC_REQUIRE(ctx, value == 1 || value == 2 || value == 4, "plan_set_option: cluster %d", value);
-    p->estep_cluster = value;
+  if (option == EMC_OPT_ESTEP_GHLO) {
+    EMC_REQUIRE(ctx, value == 0 || value == 1, "plan_set_option: gh_lo %d", value);
+    p->estep_gh_lo = value;
+    return EMC_OK;
+  }
+  if (option == EMC_OPT_MSTEP_AGGREGATE) {
+    EMC_REQUIRE(ctx, value == 0 || value == 1, "plan_set_option: aggregate %d", value);
+    p->mstep_aggregate = value;
     return EMC_OK;
   }
   if (option == EMC_OPT_MSTEP_QLO) {

@@ -75,32 +75,6 @@ __device__ __forceinline__ void tma_load_2d(void* smem_dst, const CUtensorMap* m
       : "memory");
 }
 
-// 2D tiled load written to the same shared-memory offset of every CTA in
-// `cta_mask` (this GPU's own memory; cluster multicast), each destination's
-// mbarrier at `bar`'s offset receiving the complete_tx.
-__device__ __forceinline__ void tma_load_2d_multicast(void* smem_dst, const CUtensorMap* map,
-                                                      int x, int y, uint64_t* bar,
-                                                      uint16_t cta_mask) {
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
-      ".multicast::cluster [%0], [%1, {%2, %3}], [%4], %5;" ::"r"(smem_u32(smem_dst)),
-      "l"((uint64_t)map), "r"(x), "r"(y), "r"(smem_u32(bar)), "h"(cta_mask)
-      : "memory");
-}
-
-// ---- clusters -------------------------------------------------------------
-__device__ __forceinline__ uint32_t cluster_ctarank() {
-  uint32_t r;
-  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
-  return r;
-}
-
-// Every thread of every CTA of the cluster arrives, then waits for all.
-__device__ __forceinline__ void cluster_sync() {
-  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::
-                   : "memory");
-}
-
 // ---- tcgen05 ---------------------------------------------------------------
 // Allocates ncols TMEM columns (power of two >= 32); the base address is
 // written to *dst_smem.  Executed by one full warp.
@@ -149,15 +123,6 @@ __device__ __forceinline__ void mma_commit(uint64_t* bar) {
       : "memory");
 }
 
-// As mma_commit, arriving on the mbarrier at `bar`'s offset in every CTA of
-// `cta_mask`.
-__device__ __forceinline__ void mma_commit_multicast(uint64_t* bar, uint16_t cta_mask) {
-  asm volatile(
-      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64"
-      " [%0], %1;" ::"r"(smem_u32(bar)),
-      "h"(cta_mask)
-      : "memory");
-}
 
 // 32 lanes x 16 columns of 32-bit TMEM values: lane i of the warp gets row
 // (taddr.lane + i), columns taddr.col .. +15.

@@ -85,7 +85,7 @@ constexpr float kK2Scale = 1.0f / 128.0f;  // K^2 * 2^-7 <= 2^15 for counts <= 2
 constexpr float kMSScale = 1.0f / 256.0f;  // (M' S) * 2^-8 keeps slices below 2^24 in range
 
 // Counts -> FP16 operands, rows of Kp (patterns padded to Np with zeros):
-// Kh = k, K2h + K2l = k^2 * 2^-7 exactly.
+// Kh = k, K2h + K2l = k^2 * 2^-7 exactly (K2h == nullptr: Kh only).
 __global__ void tc_pattern_ops_kernel(const float* __restrict__ images, const int* __restrict__ pix,
                                       int n2, int N, int Kp, __half* __restrict__ Kh,
                                       __half* __restrict__ K2h, __half* __restrict__ K2l) {
@@ -102,8 +102,10 @@ __global__ void tc_pattern_ops_kernel(const float* __restrict__ images, const in
   const __half lo = __float2half_rn(k2 - __half2float(hi));
   const size_t o = (size_t)i * Kp + q;
   Kh[o] = __float2half_rn(k);
-  K2h[o] = hi;
-  K2l[o] = lo;
+  if (K2h) {
+    K2h[o] = hi;
+    K2l[o] = lo;
+  }
 }
 
 // flags[pt][kb] = any K2l != 0 in rows pt*128..+127, cols kb*32..+31.
@@ -167,16 +169,38 @@ __global__ void tc_rot_ops_kernel(const float* __restrict__ S, size_t n, __half*
   }
 }
 
+// True-Poisson rotation operand: log max(s, floor) as FP16 hi + lo [Rp][Kp]
+// (|log| <= 14 for slices below 2^20; hi + lo carries ~22 bits).
+constexpr float kSliceFloorT = 1e-6f;  // the FP32 path's floor for unknown voxels
+
+__global__ void tc_rot_logs_kernel(const float* __restrict__ S, size_t n, __half* __restrict__ Lh,
+                                   __half* __restrict__ Ll) {
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += stride) {
+    const float l = logf(fmaxf(S[e], kSliceFloorT));
+    const __half hi = __float2half_rn(l);
+    Lh[e] = hi;
+    Ll[e] = __float2half_rn(l - __half2float(hi));
+  }
+}
+
 // ------------------------------------------------------------ E-step -----
+// One CTA owns 128 patterns x 128 rotations and all four contractions:
+//   B = K . G^T,  den = K . (M'S)^T,  C = K^2 . H^T,  num = K^2 . M'^T.
+// Operands that multiply the same pattern-side tile are stored next to each
+// other in shared memory ([G | M'S] and [H | M']), so each pair is one
+// 128 x 256 MMA: the pattern-side tile is read once per pair, which lowers
+// the shared-memory operand traffic per FLOP that bounds 128 x 128 MMAs.
+// TMEM columns: B 0-127, den 128-255, C 256-383, num 384-511.
 namespace es {
 constexpr int BM = 128;        // patterns per tile (TMEM lanes)
 constexpr int BN = 128;        // rotations per tile
 constexpr int BK = 32;         // pixels per stage (64 B rows, 64B swizzle)
 constexpr int STAGES = 3;
 constexpr int TILE_BYTES = 128 * BK * 2;  // 8 KB, both operand sides
-constexpr int NA = 3;          // K, K2h, K2l
-constexpr int NB = 6;          // M', MS, Gh, Gl, Hh, Hl
-constexpr int STAGE_BYTES = (NA + NB) * TILE_BYTES;
+// stage slots: pattern side, then the two N=256 pairs, then the lo terms
+enum Slot { sK = 0, sK2h, sK2l, sGh, sMS, sHh, sMp, sGl, sHl, kSlots };
+constexpr int STAGE_BYTES = kSlots * TILE_BYTES;
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 2048 + 1024;
 constexpr int THREADS = 192;
 constexpr int GROUP = 8;       // rotation tiles per raster group
@@ -184,6 +208,7 @@ constexpr int GROUP = 8;       // rotation tiles per raster group
 
 struct TcEstepArgs {
   int N, R, Kp, n_pt, n_rt, nkb;
+  int gh_lo;                      // 1: G and H as FP16 hi + lo, 0: hi only
   const unsigned char* k2lo_any;  // [n_pt][nkb]
   const float* rot_cnt;
   const float* rot_A;
@@ -198,13 +223,6 @@ struct TcEstepArgs {
   int* status;
 };
 
-// CL > 1: launched in clusters of CL CTAs that share one rotation tile and
-// hold CL consecutive pattern tiles.  Each CTA loads 128/CL rows of every
-// rotation-side tile and multicasts them to the whole cluster, so L2 serves
-// each rotation-side byte once per cluster instead of once per CTA; every
-// CTA's MMA completion is multicast to all empty barriers (arrival count
-// CL), so no stage is overwritten before the whole cluster has consumed it.
-template <int CL>
 __global__ void __launch_bounds__(es::THREADS, 1)
     tc_estep_kernel(const __grid_constant__ CUtensorMap mK, const __grid_constant__ CUtensorMap mK2h,
                     const __grid_constant__ CUtensorMap mK2l, const __grid_constant__ CUtensorMap mMp,
@@ -223,23 +241,19 @@ __global__ void __launch_bounds__(es::THREADS, 1)
   float* s_lw = s_scale + BN;
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  // grouped raster over clusters: GROUP rotation tiles share each cluster of
-  // CL pattern tiles in turn
-  const int member = CL > 1 ? (int)ptx::cluster_ctarank() : 0;
-  const int cid = blockIdx.x / CL;
-  const int n_ptc = a.n_pt / CL;
-  const int per_group = GROUP * n_ptc;
-  const int g = cid / per_group, within = cid % per_group;
+  // grouped raster: GROUP rotation tiles share each pattern tile in turn
+  const int per_group = GROUP * a.n_pt;
+  const int g = blockIdx.x / per_group, within = blockIdx.x % per_group;
   const int rt0 = g * GROUP;
   const int gsz = min(GROUP, a.n_rt - rt0);
   const int rt = rt0 + within % gsz;
-  const int pt = (within / gsz) * CL + member;
+  const int pt = within / gsz;
   const int n0 = pt * BM, r0 = rt * BN;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
       ptx::mbar_init(&full[s], 1);
-      ptx::mbar_init(&empty[s], CL);
+      ptx::mbar_init(&empty[s], 1);
     }
     ptx::mbar_init(accum, 1);
     ptx::fence_mbar_init();
@@ -257,76 +271,61 @@ __global__ void __launch_bounds__(es::THREADS, 1)
   }
   ptx::tc_fence_before();
   __syncthreads();
-  if (CL > 1) ptx::cluster_sync();  // peers' barriers exist before any multicast
   ptx::tc_fence_after();
   const uint32_t tmem = *tmem_slot;
   const unsigned char* flags = a.k2lo_any + (size_t)pt * a.nkb;
-  constexpr uint16_t kAll = (uint16_t)((1u << CL) - 1);
-  constexpr int kRows = BN / CL;  // rotation rows each cluster member fetches
+  const bool ghlo = a.gh_lo != 0;
 
   if (warp == 0) {
     // ------------------------------------------------ TMA producer
     if (lane == 0) {
-      const CUtensorMap* amap[NA] = {&mK, &mK2h, &mK2l};
-      const CUtensorMap* bmap[NB] = {&mMp, &mMS, &mGh, &mGl, &mHh, &mHl};
+      const CUtensorMap* maps[kSlots] = {&mK, &mK2h, &mK2l, &mGh, &mMS, &mHh, &mMp, &mGl, &mHl};
       for (int kb = 0; kb < a.nkb; ++kb) {
         const int s = kb % STAGES;
         const uint32_t ph = (kb / STAGES) & 1;
         if (!ptx::mbar_wait(&empty[s], ph ^ 1, a.status, 0)) break;
         const bool lo = flags[kb] != 0;
-        ptx::mbar_arrive_expect_tx(&full[s], (NA + NB - (lo ? 0 : 1)) * TILE_BYTES);
+        const int ntiles = kSlots - (lo ? 0 : 1) - (ghlo ? 0 : 2);
+        ptx::mbar_arrive_expect_tx(&full[s], ntiles * TILE_BYTES);
         unsigned char* st = smem + s * STAGE_BYTES;
-        for (int j = 0; j < NA; ++j) {
-          if (j == 2 && !lo) continue;
-          ptx::tma_load_2d(st + j * TILE_BYTES, amap[j], kb * BK, n0, &full[s]);
-        }
-        for (int j = 0; j < NB; ++j) {
-          if (CL == 1) {
-            ptx::tma_load_2d(st + (NA + j) * TILE_BYTES, bmap[j], kb * BK, r0, &full[s]);
-          } else {
-            // rows member*kRows..+kRows-1 of the tile, to the same offset in every CTA
-            ptx::tma_load_2d_multicast(st + (NA + j) * TILE_BYTES + member * kRows * BK * 2,
-                                       bmap[j], kb * BK, r0 + member * kRows, &full[s], kAll);
-          }
+        for (int j = 0; j < kSlots; ++j) {
+          if (j == sK2l && !lo) continue;
+          if ((j == sGl || j == sHl) && !ghlo) continue;
+          ptx::tma_load_2d(st + j * TILE_BYTES, maps[j], kb * BK, j < sGh ? n0 : r0, &full[s]);
         }
       }
     }
   } else if (warp == 1) {
     // ------------------------------------------------ MMA issuer
     if (lane == 0) {
-      constexpr uint32_t idesc = ptx::idesc_f16(BM, BN);
-      bool ok = true;
-      for (int kb = 0; kb < a.nkb && ok; ++kb) {
+      constexpr uint32_t idesc2 = ptx::idesc_f16(BM, 2 * BN);  // the N = 256 pairs
+      constexpr uint32_t idesc1 = ptx::idesc_f16(BM, BN);
+      for (int kb = 0; kb < a.nkb; ++kb) {
         const int s = kb % STAGES;
         const uint32_t ph = (kb / STAGES) & 1;
-        if (!ptx::mbar_wait(&full[s], ph, a.status, 1)) {
-          ok = false;
-          break;
-        }
+        if (!ptx::mbar_wait(&full[s], ph, a.status, 1)) break;
         ptx::tc_fence_after();
         const bool lo = flags[kb] != 0;
         const uint32_t base = ptx::smem_u32(smem + s * STAGE_BYTES);
 #pragma unroll
         for (int ks = 0; ks < BK / 16; ++ks) {
+          // 8-row core-matrix groups 512 B apart: a 256-row operand runs
+          // through two adjacent 128-row slots
           auto d = [&](int j) { return ptx::smem_desc(base + j * TILE_BYTES + ks * 32, 512, 4); };
-          const uint64_t aK = d(0), aK2h = d(1), aK2l = d(2);
-          const uint64_t bM = d(3), bMS = d(4), bGh = d(5), bGl = d(6), bHh = d(7), bHl = d(8);
           const uint32_t acc = (kb | ks) ? 1u : 0u;
-          ptx::mma_f16(tmem + 0, aK2h, bM, idesc, acc);  // num
-          if (lo) ptx::mma_f16(tmem + 0, aK2l, bM, idesc, 1);
-          ptx::mma_f16(tmem + 128, aK, bMS, idesc, acc);  // den
-          ptx::mma_f16(tmem + 256, aK, bGh, idesc, acc);  // B
-          ptx::mma_f16(tmem + 256, aK, bGl, idesc, 1);
-          ptx::mma_f16(tmem + 384, aK2h, bHh, idesc, acc);  // C
-          ptx::mma_f16(tmem + 384, aK2h, bHl, idesc, 1);
-          if (lo) ptx::mma_f16(tmem + 384, aK2l, bHh, idesc, 1);
+          ptx::mma_f16(tmem + 0, d(sK), d(sGh), idesc2, acc);      // B hi | den
+          ptx::mma_f16(tmem + 256, d(sK2h), d(sHh), idesc2, acc);  // C hi | num
+          if (ghlo) {
+            ptx::mma_f16(tmem + 0, d(sK), d(sGl), idesc1, 1u);     // B lo
+            ptx::mma_f16(tmem + 256, d(sK2h), d(sHl), idesc1, 1u); // C lo
+          }
+          if (lo) ptx::mma_f16(tmem + 256, d(sK2l), d(sHh), idesc2, 1u);  // K^2 lo: C | num
         }
-        if (CL == 1)
-          ptx::mma_commit(&empty[s]);
-        else
-          ptx::mma_commit_multicast(&empty[s], kAll);  // frees the stage in every CTA
+        ptx::mma_commit(&empty[s]);
       }
-      ptx::mma_commit(accum);  // fires when every MMA above has completed
+      // fires when every MMA issued above has completed; after a timeout the
+      // epilogue's own bounded wait reports it
+      ptx::mma_commit(accum);
     }
   } else {
     // ------------------------------------------------ epilogue (warps 2-5)
@@ -342,10 +341,10 @@ __global__ void __launch_bounds__(es::THREADS, 1)
       const uint32_t lane_addr = tmem + ((uint32_t)(quarter * 32) << 16);
       for (int c0 = 0; c0 < BN; c0 += 16) {
         float vn[16], vd[16], vb[16], vc[16];
-        ptx::tmem_ld16(lane_addr + 0 + c0, vn);
+        ptx::tmem_ld16(lane_addr + 0 + c0, vb);
         ptx::tmem_ld16(lane_addr + 128 + c0, vd);
-        ptx::tmem_ld16(lane_addr + 256 + c0, vb);
-        ptx::tmem_ld16(lane_addr + 384 + c0, vc);
+        ptx::tmem_ld16(lane_addr + 256 + c0, vc);
+        ptx::tmem_ld16(lane_addr + 384 + c0, vn);
         ptx::tmem_wait_ld();
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
@@ -386,9 +385,180 @@ __global__ void __launch_bounds__(es::THREADS, 1)
     ptx::tc_fence_after();
     ptx::tmem_dealloc(tmem, 512);
   }
-  // peers may still multicast MMA completions to this CTA's empty barriers
-  // until their last MMA retires: leave only together
-  if (CL > 1) ptx::cluster_sync();
+}
+
+// ------------------------------------------------ E-step, true Poisson -----
+// L_ri = log w_r + c_i sum_p k_ip log s~_rp + K_i log(K_i / S_r) - K_i,
+// s~ = max(s, floor), K_i = c_i sum_p k_ip, S_r = sum_p s~_rp, phi = K_i / S_r
+// (known intensity: phi = 1, L = log w_r + c_i sum k log s~ - S_r), as the
+// FP32 path.  One contraction K . (log S~)^T with log S~ as FP16 hi + lo;
+// one CTA owns 128 patterns x 256 rotations (TMEM columns 0-255) and writes
+// one (max, sum exp) partial per 128-rotation half.
+namespace ep {
+constexpr int BM = 128;   // patterns per tile (TMEM lanes)
+constexpr int BN = 256;   // rotations per tile
+constexpr int BK = 32;    // pixels per stage (64 B rows, 64B swizzle)
+constexpr int STAGES = 4;
+constexpr int A_BYTES = BM * BK * 2;  // 8 KB
+constexpr int B_BYTES = BN * BK * 2;  // 16 KB
+constexpr int STAGE_BYTES = A_BYTES + 2 * B_BYTES;
+constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 256 + 2 * BN * 4 + 1024;
+constexpr int THREADS = 192;
+constexpr int GROUP = 8;
+}  // namespace ep
+
+struct TcEstepPoisArgs {
+  int N, R, n_pt, n_rt, nkb;
+  int n_part;             // 128-rotation partial tiles
+  const float* rot_ssum;  // S_r
+  const float* rotw;
+  const float* Ksum;      // K_i (normalised counts)
+  const float* cnorm;     // c_i
+  int known_intensity;
+  float* L;
+  float* PHI;
+  float2* part;
+  int* status;
+};
+
+__global__ void __launch_bounds__(ep::THREADS, 1)
+    tc_estep_pois_kernel(const __grid_constant__ CUtensorMap mK,
+                         const __grid_constant__ CUtensorMap mLh,
+                         const __grid_constant__ CUtensorMap mLl, TcEstepPoisArgs a) {
+  using namespace ep;
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint64_t* full = (uint64_t*)(smem + STAGES * STAGE_BYTES);
+  uint64_t* empty = full + STAGES;
+  uint64_t* accum = empty + STAGES;
+  uint32_t* tmem_slot = (uint32_t*)(accum + 1);
+  float* s_ss = (float*)(smem + STAGES * STAGE_BYTES + 256);
+  float* s_lw = s_ss + BN;
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int per_group = GROUP * a.n_pt;
+  const int g = blockIdx.x / per_group, within = blockIdx.x % per_group;
+  const int rt0 = g * GROUP;
+  const int gsz = min(GROUP, a.n_rt - rt0);
+  const int rt = rt0 + within % gsz;
+  const int pt = within / gsz;
+  const int n0 = pt * BM, r0 = rt * BN;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      ptx::mbar_init(&full[s], 1);
+      ptx::mbar_init(&empty[s], 1);
+    }
+    ptx::mbar_init(accum, 1);
+    ptx::fence_mbar_init();
+  }
+  for (int c = threadIdx.x; c < BN; c += blockDim.x) {
+    const int r = r0 + c;
+    s_ss[c] = r < a.R ? a.rot_ssum[r] : 1.0f;
+    s_lw[c] = r < a.R ? logf(a.rotw[r]) : 0.0f;
+  }
+  if (warp == 1) {
+    ptx::tmem_alloc(tmem_slot, BN);
+    ptx::tmem_relinquish();
+  }
+  ptx::tc_fence_before();
+  __syncthreads();
+  ptx::tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0) {
+    // ------------------------------------------------ TMA producer
+    if (lane == 0) {
+      for (int kb = 0; kb < a.nkb; ++kb) {
+        const int s = kb % STAGES;
+        const uint32_t ph = (kb / STAGES) & 1;
+        if (!ptx::mbar_wait(&empty[s], ph ^ 1, a.status, 8)) break;
+        ptx::mbar_arrive_expect_tx(&full[s], STAGE_BYTES);
+        unsigned char* st = smem + s * STAGE_BYTES;
+        ptx::tma_load_2d(st, &mK, kb * BK, n0, &full[s]);
+        ptx::tma_load_2d(st + A_BYTES, &mLh, kb * BK, r0, &full[s]);
+        ptx::tma_load_2d(st + A_BYTES + B_BYTES, &mLl, kb * BK, r0, &full[s]);
+      }
+    }
+  } else if (warp == 1) {
+    // ------------------------------------------------ MMA issuer
+    if (lane == 0) {
+      constexpr uint32_t idesc = ptx::idesc_f16(BM, BN);
+      for (int kb = 0; kb < a.nkb; ++kb) {
+        const int s = kb % STAGES;
+        const uint32_t ph = (kb / STAGES) & 1;
+        if (!ptx::mbar_wait(&full[s], ph, a.status, 9)) break;
+        ptx::tc_fence_after();
+        const uint32_t base = ptx::smem_u32(smem + s * STAGE_BYTES);
+#pragma unroll
+        for (int ks = 0; ks < BK / 16; ++ks) {
+          const uint64_t aK = ptx::smem_desc(base + ks * 32, 512, 4);
+          const uint64_t bh = ptx::smem_desc(base + A_BYTES + ks * 32, 512, 4);
+          const uint64_t bl = ptx::smem_desc(base + A_BYTES + B_BYTES + ks * 32, 512, 4);
+          ptx::mma_f16(tmem, aK, bh, idesc, (kb | ks) ? 1u : 0u);
+          ptx::mma_f16(tmem, aK, bl, idesc, 1u);
+        }
+        ptx::mma_commit(&empty[s]);
+      }
+      ptx::mma_commit(accum);
+    }
+  } else {
+    // ------------------------------------------------ epilogue (warps 2-5)
+    const int quarter = warp & 3;
+    const int row = quarter * 32 + lane;
+    const int n = n0 + row;
+    const bool nok = n < a.N;
+    const float ci = nok ? a.cnorm[n] : 1.0f;
+    const float Ki = nok ? a.Ksum[n] : 0.0f;
+    const bool waited = ptx::mbar_wait(accum, 0, a.status, 10);
+    if (waited) ptx::tc_fence_after();
+    const uint32_t lane_addr = tmem + ((uint32_t)(quarter * 32) << 16);
+    for (int h = 0; h < 2; ++h) {
+      float m = -INFINITY, ssum = 0.0f;
+      for (int c0 = h * 128; waited && c0 < h * 128 + 128; c0 += 16) {
+        float v[16];
+        ptx::tmem_ld16(lane_addr + c0, v);
+        ptx::tmem_wait_ld();
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          const int cl = c0 + j;
+          const int r = r0 + cl;
+          const float acc = ci * v[j];
+          float l, f;
+          if (a.known_intensity) {
+            f = 1.0f;
+            l = s_lw[cl] + acc - s_ss[cl];
+          } else if (Ki > 0.0f) {
+            f = Ki / s_ss[cl];
+            l = s_lw[cl] + acc + Ki * logf(f) - Ki;
+          } else {
+            f = 0.0f;
+            l = s_lw[cl];
+          }
+          const bool ok = nok && r < a.R;
+          if (ok) {
+            a.L[(size_t)r * a.N + n] = l;
+            a.PHI[(size_t)r * a.N + n] = f;
+          }
+          const float L = ok ? l : -INFINITY;
+          if (L > m) {
+            ssum = ssum * expf(m - L) + 1.0f;
+            m = L;
+          } else if (L > -INFINITY) {
+            ssum += expf(L - m);
+          }
+        }
+      }
+      const int t = 2 * rt + h;
+      if (nok && t < a.n_part) a.part[(size_t)t * a.N + n] = make_float2(m, ssum);
+    }
+  }
+  ptx::tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    ptx::tc_fence_after();
+    ptx::tmem_dealloc(tmem, BN);
+  }
 }
 
 // ------------------------------------------------------------ M-step -----
@@ -400,18 +570,20 @@ constexpr int STAGES = 3;
 constexpr int A_BYTES = BM * BK * 2;  // 16 KB
 constexpr int B_BYTES = BN * BK * 2;  // 32 KB
 constexpr int STAGE_BYTES = 2 * A_BYTES + B_BYTES;
-constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 1024 + BM * (int)sizeof(RotMat);
-constexpr int THREADS = 192;
+constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 256 + 1024;
+constexpr int EPI_WARPS = 8;          // two per TMEM lane quarter, 128 columns each
+constexpr int THREADS = 64 + 32 * EPI_WARPS;
 constexpr int GROUP = 8;
 }  // namespace ms
 
 struct TcMstepArgs {
-  int R, Kp, Np, P_eff, n_qt, n_rt, nkb;
+  int R, Kp, Np, P_eff, n_qt, n_rt, nkb, n_tiles;
   const float* T;
   const float* qscale;  // [R] 2^-e_r
   const float* rot;
   const float *cx, *cy, *cz;
   int side, interp, deterministic;
+  int aggregate;  // 1: lanes hitting the same voxel combine before one atomic
   float* model;
   float* weight;
   unsigned long long* fix_m;
@@ -435,16 +607,45 @@ __device__ __forceinline__ void tc_add(const TcMstepArgs& a, size_t v, float val
   }
 }
 
-__device__ __forceinline__ void tc_insert(const TcMstepArgs& a, const RotMat& R, float x, float y,
-                                          float z, float val, float w) {
+// Nearest-voxel insertion of one value per lane.  With aggregation (float
+// atomics only), lanes of the warp whose voxels coincide -- neighbouring
+// rotations at the same small-radius pixel -- add their values in registers
+// and their lowest lane issues one atomic.  Called by all 32 lanes.
+__device__ __forceinline__ void tc_insert_nearest(const TcMstepArgs& a, bool on, long long v,
+                                                  float val, float w) {
+  if (a.aggregate && !a.deterministic) {
+    const unsigned act = __ballot_sync(0xffffffffu, on);
+    if (!on) return;
+    const unsigned peers = __match_any_sync(act, v);
+    const int me = threadIdx.x & 31;
+    const int leader = __ffs(peers) - 1;
+    // every lane of a peer group runs the same sequence of shuffles
+    for (unsigned m = peers & (peers - 1); m; m &= m - 1) {
+      const int src = __ffs(m) - 1;
+      const float pv = __shfl_sync(peers, val, src);
+      const float pw = __shfl_sync(peers, w, src);
+      if (me == leader) {
+        val += pv;
+        w += pw;
+      }
+    }
+    if (me == leader) atomicAdd(a.acc2 + v, make_float2(val, w));
+    return;
+  }
+  if (on) tc_add(a, (size_t)v, val, w);
+}
+
+__device__ __forceinline__ void tc_insert(const TcMstepArgs& a, const RotMat& R, bool on, float x,
+                                          float y, float z, float val, float w) {
   const int side = a.side;
   if (a.interp == EMC_INTERP_NEAREST) {
     const long ix = lroundf(voxel_coord(side, rotate_row(R, 0, x, y, z)));
     const long iy = lroundf(voxel_coord(side, rotate_row(R, 1, x, y, z)));
     const long iz = lroundf(voxel_coord(side, rotate_row(R, 2, x, y, z)));
-    if (ix < 0 || ix >= side || iy < 0 || iy >= side || iz < 0 || iz >= side) return;
-    tc_add(a, ((size_t)iz * side + iy) * side + ix, val, w);
+    const bool in = on && ix >= 0 && ix < side && iy >= 0 && iy < side && iz >= 0 && iz < side;
+    tc_insert_nearest(a, in, in ? ((long long)iz * side + iy) * side + ix : -1, val, w);
   } else {
+    if (!on) return;
     const float cx = voxel_coord(side, rotate_row(R, 0, x, y, z));
     const float cy = voxel_coord(side, rotate_row(R, 1, x, y, z));
     const float cz = voxel_coord(side, rotate_row(R, 2, x, y, z));
@@ -463,6 +664,20 @@ __device__ __forceinline__ void tc_insert(const TcMstepArgs& a, const RotMat& R,
   }
 }
 
+// Tile t of the grouped raster: GROUP rotation tiles share each pixel tile.
+__device__ __forceinline__ void ms_tile(const TcMstepArgs& a, int t, int& r0, int& q0) {
+  const int per_group = ms::GROUP * a.n_qt;
+  const int g = t / per_group, within = t % per_group;
+  const int rt0 = g * ms::GROUP;
+  const int gsz = min(ms::GROUP, a.n_rt - rt0);
+  r0 = (rt0 + within % gsz) * ms::BM;
+  q0 = (within / gsz) * ms::BN;
+}
+
+// Persistent: CTA b takes tiles b, b + grid, ...  The k-block ring runs on
+// across tiles, and the accumulator is double-buffered in TMEM (columns
+// 0-255 and 256-511), so the insertion epilogue of one tile overlaps the
+// MMAs of the next.
 __global__ void __launch_bounds__(ms::THREADS, 1)
     tc_mstep_kernel(const __grid_constant__ CUtensorMap mQh, const __grid_constant__ CUtensorMap mQl,
                     const __grid_constant__ CUtensorMap mKt, TcMstepArgs a) {
@@ -471,34 +686,24 @@ __global__ void __launch_bounds__(ms::THREADS, 1)
   unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   uint64_t* full = (uint64_t*)(smem + STAGES * STAGE_BYTES);
   uint64_t* empty = full + STAGES;
-  uint64_t* accum = empty + STAGES;
-  uint32_t* tmem_slot = (uint32_t*)(accum + 1);
-  RotMat* sR = (RotMat*)(smem + STAGES * STAGE_BYTES + 1024);
+  uint64_t* tfull = empty + STAGES;  // [2] accumulator ready
+  uint64_t* tempty = tfull + 2;      // [2] accumulator drained (one arrival per epilogue warp)
+  uint32_t* tmem_slot = (uint32_t*)(tempty + 2);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int t = blockIdx.x;
-  const int per_group = GROUP * a.n_qt;
-  const int g = t / per_group, within = t % per_group;
-  const int rt0 = g * GROUP;
-  const int gsz = min(GROUP, a.n_rt - rt0);
-  const int rt = rt0 + within % gsz;
-  const int qt = within / gsz;
-  const int r0 = rt * BM, q0 = qt * BN;
-
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
       ptx::mbar_init(&full[s], 1);
       ptx::mbar_init(&empty[s], 1);
     }
-    ptx::mbar_init(accum, 1);
+    for (int b = 0; b < 2; ++b) {
+      ptx::mbar_init(&tfull[b], 1);
+      ptx::mbar_init(&tempty[b], EPI_WARPS);
+    }
     ptx::fence_mbar_init();
   }
-  if (threadIdx.x < BM) {
-    const int r = r0 + threadIdx.x;
-    if (r < a.R) sR[threadIdx.x] = quat_to_matrix(a.rot + 4 * (size_t)r);
-  }
   if (warp == 1) {
-    ptx::tmem_alloc(tmem_slot, 256);
+    ptx::tmem_alloc(tmem_slot, 512);
     ptx::tmem_relinquish();
   }
   ptx::tc_fence_before();
@@ -507,79 +712,117 @@ __global__ void __launch_bounds__(ms::THREADS, 1)
   const uint32_t tmem = *tmem_slot;
 
   if (warp == 0) {
+    // ------------------------------------------------ TMA producer
     if (lane == 0) {
-      for (int kb = 0; kb < a.nkb; ++kb) {
-        const int s = kb % STAGES;
-        const uint32_t ph = (kb / STAGES) & 1;
-        if (!ptx::mbar_wait(&empty[s], ph ^ 1, a.status, 4)) break;
-        ptx::mbar_arrive_expect_tx(&full[s], STAGE_BYTES - (a.q_lo ? 0 : A_BYTES));
-        unsigned char* st = smem + s * STAGE_BYTES;
-        ptx::tma_load_2d(st, &mQh, kb * BK, r0, &full[s]);
-        if (a.q_lo) ptx::tma_load_2d(st + A_BYTES, &mQl, kb * BK, r0, &full[s]);
-        ptx::tma_load_2d(st + 2 * A_BYTES, &mKt, kb * BK, q0, &full[s]);
+      uint32_t it = 0;
+      bool ok = true;
+      for (int t = blockIdx.x; t < a.n_tiles && ok; t += gridDim.x) {
+        int r0, q0;
+        ms_tile(a, t, r0, q0);
+        for (int kb = 0; kb < a.nkb; ++kb, ++it) {
+          const int s = it % STAGES;
+          const uint32_t ph = (it / STAGES) & 1;
+          if (!ptx::mbar_wait(&empty[s], ph ^ 1, a.status, 4)) {
+            ok = false;
+            break;
+          }
+          ptx::mbar_arrive_expect_tx(&full[s], STAGE_BYTES - (a.q_lo ? 0 : A_BYTES));
+          unsigned char* st = smem + s * STAGE_BYTES;
+          ptx::tma_load_2d(st, &mQh, kb * BK, r0, &full[s]);
+          if (a.q_lo) ptx::tma_load_2d(st + A_BYTES, &mQl, kb * BK, r0, &full[s]);
+          ptx::tma_load_2d(st + 2 * A_BYTES, &mKt, kb * BK, q0, &full[s]);
+        }
       }
     }
   } else if (warp == 1) {
+    // ------------------------------------------------ MMA issuer
     if (lane == 0) {
       constexpr uint32_t idesc = ptx::idesc_f16(BM, BN);
-      for (int kb = 0; kb < a.nkb; ++kb) {
-        const int s = kb % STAGES;
-        const uint32_t ph = (kb / STAGES) & 1;
-        if (!ptx::mbar_wait(&full[s], ph, a.status, 5)) break;
+      uint32_t it = 0;
+      bool ok = true;
+      int j = 0;
+      for (int t = blockIdx.x; t < a.n_tiles && ok; t += gridDim.x, ++j) {
+        const int b = j & 1;
+        const uint32_t d = tmem + (uint32_t)(b * BN);
+        if (!ptx::mbar_wait(&tempty[b], ((j >> 1) & 1) ^ 1, a.status, 7)) break;
         ptx::tc_fence_after();
-        const uint32_t base = ptx::smem_u32(smem + s * STAGE_BYTES);
+        for (int kb = 0; kb < a.nkb; ++kb, ++it) {
+          const int s = it % STAGES;
+          const uint32_t ph = (it / STAGES) & 1;
+          if (!ptx::mbar_wait(&full[s], ph, a.status, 5)) {
+            ok = false;
+            break;
+          }
+          ptx::tc_fence_after();
+          const uint32_t base = ptx::smem_u32(smem + s * STAGE_BYTES);
 #pragma unroll
-        for (int ks = 0; ks < BK / 16; ++ks) {
-          const uint64_t dQh = ptx::smem_desc(base + ks * 32, 1024, 2);
-          const uint64_t dQl = ptx::smem_desc(base + A_BYTES + ks * 32, 1024, 2);
-          const uint64_t dK = ptx::smem_desc(base + 2 * A_BYTES + ks * 32, 1024, 2);
-          ptx::mma_f16(tmem, dQh, dK, idesc, (kb | ks) ? 1u : 0u);
-          if (a.q_lo) ptx::mma_f16(tmem, dQl, dK, idesc, 1u);
+          for (int ks = 0; ks < BK / 16; ++ks) {
+            const uint64_t dQh = ptx::smem_desc(base + ks * 32, 1024, 2);
+            const uint64_t dQl = ptx::smem_desc(base + A_BYTES + ks * 32, 1024, 2);
+            const uint64_t dK = ptx::smem_desc(base + 2 * A_BYTES + ks * 32, 1024, 2);
+            ptx::mma_f16(d, dQh, dK, idesc, (kb | ks) ? 1u : 0u);
+            if (a.q_lo) ptx::mma_f16(d, dQl, dK, idesc, 1u);
+          }
+          ptx::mma_commit(&empty[s]);
         }
-        ptx::mma_commit(&empty[s]);
+        ptx::mma_commit(&tfull[b]);  // fires when this tile's MMAs have completed
       }
-      ptx::mma_commit(accum);
     }
   } else {
-    const int quarter = warp & 3;
+    // ------------------------------------------------ insertion epilogue (warps 2-9)
+    const int quarter = warp & 3;       // TMEM lanes this warp may access
+    const int half = (warp - 2) >> 2;   // which 128 of the tile's 256 columns
     const int rl = quarter * 32 + lane;
-    const int r = r0 + rl;
-    const bool rok = r < a.R;
-    const float Tr = rok ? a.T[r] : 0.0f;
-    const float qs = rok ? a.qscale[r] : 0.0f;
-    const bool live = rok && Tr > 1e-10f;
-    if (ptx::mbar_wait(accum, 0, a.status, 6)) {
+    int j = 0;
+    for (int t = blockIdx.x; t < a.n_tiles; t += gridDim.x, ++j) {
+      const int b = j & 1;
+      int r0, q0;
+      ms_tile(a, t, r0, q0);
+      const int r = r0 + rl;
+      const bool rok = r < a.R;
+      const float Tr = rok ? a.T[r] : 0.0f;
+      const float qs = rok ? a.qscale[r] : 0.0f;
+      const bool live = rok && Tr > 1e-10f;
+      RotMat Rm = {};
+      if (rok) Rm = quat_to_matrix(a.rot + 4 * (size_t)r);
+      if (!ptx::mbar_wait(&tfull[b], (j >> 1) & 1, a.status, 6)) break;
       ptx::tc_fence_after();
-      const RotMat Rm = sR[rl];
-      const uint32_t lane_addr = tmem + ((uint32_t)(quarter * 32) << 16);
-      for (int c0 = 0; c0 < BN; c0 += 16) {
+      const uint32_t lane_addr = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(b * BN);
+      for (int c0 = half * 128; c0 < half * 128 + 128; c0 += 16) {
         float u[16];
         ptx::tmem_ld16(lane_addr + c0, u);
         ptx::tmem_wait_ld();
-        if (!live) continue;
-#pragma unroll 4
-        for (int j = 0; j < 16; ++j) {
-          const int q = q0 + c0 + j;
-          if (q >= a.P_eff) break;
-          const float U = u[j] * qs;
-          const float slice = U / Tr;
-          tc_insert(a, Rm, __ldg(a.cx + q), __ldg(a.cy + q), __ldg(a.cz + q), Tr * slice, Tr);
+        if (q0 + c0 >= a.P_eff) continue;  // padding columns (uniform over the warp)
+#pragma unroll
+        for (int jj = 0; jj < 16; ++jj) {  // fully unrolled: u[] stays in registers
+          const int q = q0 + c0 + jj;
+          if (q < a.P_eff) {  // uniform over the warp
+            const float U = u[jj] * qs;
+            const float slice = live ? U / Tr : 0.0f;
+            tc_insert(a, Rm, live, __ldg(a.cx + q), __ldg(a.cy + q), __ldg(a.cz + q), Tr * slice,
+                      Tr);
+          }
         }
       }
+      // this warp's reads of buffer b are complete: hand it back to the MMA warp
+      ptx::tc_fence_before();
+      __syncwarp();
+      if (lane == 0) ptx::mbar_arrive(&tempty[b]);
     }
   }
   ptx::tc_fence_before();
   __syncthreads();
   if (warp == 1) {
     ptx::tc_fence_after();
-    ptx::tmem_dealloc(tmem, 256);
+    ptx::tmem_dealloc(tmem, 512);
   }
 }
 
 // ------------------------------------------------------------ host -------
 struct TcState {
   CUtensorMap mK, mK2h, mK2l, mQh, mQl, mKt;
-  CUtensorMap rot[3][6];  // rotation-side maps, box rows 128 / {1, 2, 4}
+  CUtensorMap rot[6];    // M', MS, Gh, Gl, Hh, Hl: 128-row boxes
+  CUtensorMap mLh, mLl;  // true Poisson: log-slices hi / lo (in Gh, Gl), 256-row boxes
   __half *Mp, *MSh, *Gh, *Gl, *Hh, *Hl;
   int* status;
 };
@@ -591,8 +834,10 @@ int tc_bind(emc_plan* p) {
   if (!p->counts_fp16_exact)
     return fail(ctx, EMC_ERR_UNSUPPORTED,
                 "mixed precision needs integer counts in [0, 2048] (exact in FP16)");
-  if (p->d.diff != EMC_DIFF_POISSON)
-    return fail(ctx, EMC_ERR_UNSUPPORTED, "mixed precision implements the reference poisson diff");
+  if (p->d.diff != EMC_DIFF_POISSON && p->d.diff != EMC_DIFF_TRUE_POISSON)
+    return fail(ctx, EMC_ERR_UNSUPPORTED,
+                "mixed precision implements the poisson and true-poisson likelihoods");
+  const bool pois = p->d.diff == EMC_DIFF_TRUE_POISSON;
   const int N = p->d.n_images, Np = p->Np, Kp = p->Kp, Rp = p->Rp;
   int rc = EMC_OK;
   if (!p->tc) {
@@ -601,13 +846,15 @@ int tc_bind(emc_plan* p) {
     p->tc = st;
     const size_t pk = (size_t)Np * Kp, rk = (size_t)Rp * Kp;
     if (!rc) rc = plan_alloc(p, (void**)&p->Kh, pk * 2);
-    if (!rc) rc = plan_alloc(p, (void**)&p->K2hi, pk * 2);
-    if (!rc) rc = plan_alloc(p, (void**)&p->K2lo, pk * 2);
     if (!rc) rc = plan_alloc(p, (void**)&p->KhT, pk * 2);
-    if (!rc) rc = plan_alloc(p, (void**)&p->k2lo_any, (size_t)(Np / 128) * (Kp / 32));
-    __half** rot_ops[6] = {&st->Mp, &st->MSh, &st->Gh, &st->Gl, &st->Hh, &st->Hl};
-    for (auto pp : rot_ops)
-      if (!rc) rc = plan_alloc(p, (void**)pp, rk * 2);
+    if (!pois) {
+      if (!rc) rc = plan_alloc(p, (void**)&p->K2hi, pk * 2);
+      if (!rc) rc = plan_alloc(p, (void**)&p->K2lo, pk * 2);
+      if (!rc) rc = plan_alloc(p, (void**)&p->k2lo_any, (size_t)(Np / 128) * (Kp / 32));
+    }
+    __half** rot_ops[6] = {&st->Gh, &st->Gl, &st->Mp, &st->MSh, &st->Hh, &st->Hl};
+    for (int j = 0; j < (pois ? 2 : 6); ++j)
+      if (!rc) rc = plan_alloc(p, (void**)rot_ops[j], rk * 2);
     if (!rc) rc = plan_alloc(p, (void**)&p->Qh, (size_t)Rp * Np * 2);
     if (!rc) rc = plan_alloc(p, (void**)&p->Ql, (size_t)Rp * Np * 2);
     if (!rc) rc = plan_alloc(p, (void**)&p->qscale, (size_t)Rp * 4);
@@ -617,28 +864,30 @@ int tc_bind(emc_plan* p) {
     EMC_CUDA(ctx, cudaMemsetAsync(p->Ql, 0, (size_t)Rp * Np * 2, ctx->stream));
     // tensor maps (fixed addresses for the plan's lifetime)
     if (!rc) rc = make_map(ctx, &st->mK, p->Kh, Np, Kp, 128, 32);
-    if (!rc) rc = make_map(ctx, &st->mK2h, p->K2hi, Np, Kp, 128, 32);
-    if (!rc) rc = make_map(ctx, &st->mK2l, p->K2lo, Np, Kp, 128, 32);
-    const __half* ro[6] = {st->Mp, st->MSh, st->Gh, st->Gl, st->Hh, st->Hl};
-    for (int c = 0; c < 3; ++c)
-      for (int j = 0; j < 6 && !rc; ++j) rc = make_map(ctx, &st->rot[c][j], ro[j], Rp, Kp, 128 >> c, 32);
+    if (pois) {
+      if (!rc) rc = make_map(ctx, &st->mLh, st->Gh, Rp, Kp, 256, 32);
+      if (!rc) rc = make_map(ctx, &st->mLl, st->Gl, Rp, Kp, 256, 32);
+    } else {
+      if (!rc) rc = make_map(ctx, &st->mK2h, p->K2hi, Np, Kp, 128, 32);
+      if (!rc) rc = make_map(ctx, &st->mK2l, p->K2lo, Np, Kp, 128, 32);
+      const __half* ro[6] = {st->Mp, st->MSh, st->Gh, st->Gl, st->Hh, st->Hl};
+      for (int j = 0; j < 6 && !rc; ++j) rc = make_map(ctx, &st->rot[j], ro[j], Rp, Kp, 128, 32);
+    }
     if (!rc) rc = make_map(ctx, &st->mQh, p->Qh, Rp, Np, 128, 64);
     if (!rc) rc = make_map(ctx, &st->mQl, p->Ql, Rp, Np, 128, 64);
     if (!rc) rc = make_map(ctx, &st->mKt, p->KhT, Kp, Np, 256, 64);
     if (rc) return rc;
-    EMC_CUDA(ctx, cudaFuncSetAttribute(tc_estep_kernel<1>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, es::SMEM_BYTES));
-    EMC_CUDA(ctx, cudaFuncSetAttribute(tc_estep_kernel<2>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, es::SMEM_BYTES));
-    EMC_CUDA(ctx, cudaFuncSetAttribute(tc_estep_kernel<4>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, es::SMEM_BYTES));
+    EMC_CUDA(ctx, cudaFuncSetAttribute(tc_estep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       es::SMEM_BYTES));
+    EMC_CUDA(ctx, cudaFuncSetAttribute(tc_estep_pois_kernel,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, ep::SMEM_BYTES));
     EMC_CUDA(ctx, cudaFuncSetAttribute(tc_mstep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        ms::SMEM_BYTES));
   }
   tc_pattern_ops_kernel<<<dim3(ceil_div(Kp, 256), Np), 256, 0, ctx->stream>>>(
-      p->images, p->pix, p->n2, N, Kp, p->Kh, p->K2hi, p->K2lo);
+      p->images, p->pix, p->n2, N, Kp, p->Kh, pois ? nullptr : p->K2hi, p->K2lo);
   if ((rc = after_launch(ctx, "tc_pattern_ops_kernel"))) return rc;
-  tc_k2lo_flags_kernel<<<dim3(Kp / 32, Np / 128), 256, 0, ctx->stream>>>(p->K2lo, Kp, p->k2lo_any,
+  if (!pois) tc_k2lo_flags_kernel<<<dim3(Kp / 32, Np / 128), 256, 0, ctx->stream>>>(p->K2lo, Kp, p->k2lo_any,
                                                                          Kp / 32);
   if ((rc = after_launch(ctx, "tc_k2lo_flags_kernel"))) return rc;
   transpose_h_kernel<<<dim3(ceil_div(Kp, 32), ceil_div(Np, 32)), dim3(32, 8), 0, ctx->stream>>>(
@@ -659,7 +908,37 @@ static int check_status(emc_plan* p, const char* what) {
   return EMC_OK;
 }
 
+static int tc_estep_pois(emc_plan* p) {
+  emc_ctx* ctx = p->ctx;
+  TcState* st = state(p);
+  const size_t rk = (size_t)p->Rp * p->Kp;
+  int rc;
+  tc_rot_logs_kernel<<<ctx->sm_count * 8, 256, 0, ctx->stream>>>(p->S, rk, st->Gh, st->Gl);
+  if ((rc = after_launch(ctx, "tc_rot_logs_kernel"))) return rc;
+  EMC_CUDA(ctx, cudaMemsetAsync(st->status, 0, sizeof(int), ctx->stream));
+  TcEstepPoisArgs a;
+  a.N = p->d.n_images;
+  a.R = p->d.n_rot;
+  a.n_pt = p->Np / ep::BM;
+  a.n_rt = ceil_div(p->Rp, ep::BN);
+  a.nkb = p->Kp / ep::BK;
+  a.n_part = p->n_rt;
+  a.rot_ssum = p->rot_ssum;
+  a.rotw = p->rotw;
+  a.Ksum = p->Ksum;
+  a.cnorm = p->cnorm;
+  a.known_intensity = p->d.known_intensity;
+  a.L = p->L;
+  a.PHI = p->PHI;
+  a.part = p->part;
+  a.status = st->status;
+  tc_estep_pois_kernel<<<a.n_pt * a.n_rt, ep::THREADS, ep::SMEM_BYTES, ctx->stream>>>(
+      st->mK, st->mLh, st->mLl, a);
+  return after_launch(ctx, "tc_estep_pois_kernel");
+}
+
 int tc_estep(emc_plan* p, float sigma) {
+  if (p->d.diff == EMC_DIFF_TRUE_POISSON) return tc_estep_pois(p);
   emc_ctx* ctx = p->ctx;
   TcState* st = state(p);
   const size_t rk = (size_t)p->Rp * p->Kp;
@@ -675,6 +954,7 @@ int tc_estep(emc_plan* p, float sigma) {
   a.n_pt = p->Np / es::BM;
   a.n_rt = p->Rp / es::BN;
   a.nkb = p->Kp / es::BK;
+  a.gh_lo = p->estep_gh_lo;
   a.k2lo_any = p->k2lo_any;
   a.rot_cnt = p->rot_cnt;
   a.rot_A = p->rot_A;
@@ -687,31 +967,10 @@ int tc_estep(emc_plan* p, float sigma) {
   a.part = p->part;
   a.bad = p->flags + 4;
   a.status = st->status;
-  const int cl = p->estep_cluster;
-  const int c = cl == 4 ? 2 : cl == 2 ? 1 : 0;
-  const CUtensorMap* rm = st->rot[c];
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(a.n_pt * a.n_rt);
-  cfg.blockDim = dim3(es::THREADS);
-  cfg.dynamicSmemBytes = es::SMEM_BYTES;
-  cfg.stream = ctx->stream;
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeClusterDimension;
-  attr[0].val.clusterDim.x = cl;
-  attr[0].val.clusterDim.y = 1;
-  attr[0].val.clusterDim.z = 1;
-  cfg.attrs = attr;
-  cfg.numAttrs = 1;
-  cudaError_t e;
-  if (cl == 4)
-    e = cudaLaunchKernelEx(&cfg, tc_estep_kernel<4>, st->mK, st->mK2h, st->mK2l, rm[0], rm[1],
-                           rm[2], rm[3], rm[4], rm[5], a);
-  else if (cl == 2)
-    e = cudaLaunchKernelEx(&cfg, tc_estep_kernel<2>, st->mK, st->mK2h, st->mK2l, rm[0], rm[1],
-                           rm[2], rm[3], rm[4], rm[5], a);
-  else
-    e = cudaLaunchKernelEx(&cfg, tc_estep_kernel<1>, st->mK, st->mK2h, st->mK2l, rm[0], rm[1],
-                           rm[2], rm[3], rm[4], rm[5], a);
+  const CUtensorMap* rm = st->rot;
+  tc_estep_kernel<<<a.n_pt * a.n_rt, es::THREADS, es::SMEM_BYTES, ctx->stream>>>(
+      st->mK, st->mK2h, st->mK2l, rm[0], rm[1], rm[2], rm[3], rm[4], rm[5], a);
+  const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(ctx, e, "tc_estep_kernel launch");
   return after_launch(ctx, "tc_estep_kernel");
 }
@@ -743,10 +1002,12 @@ int tc_mstep(emc_plan* p, float* model, float* weight) {
   a.fix_w = p->fix_w;
   a.acc2 = p->acc2;
   a.q_lo = p->mstep_q_lo;
+  a.aggregate = p->mstep_aggregate;
   a.bounds = p->red + kRedBoundM;
   a.status = st->status;
-  const int tiles = a.n_qt * a.n_rt;
-  tc_mstep_kernel<<<tiles, ms::THREADS, ms::SMEM_BYTES, ctx->stream>>>(st->mQh, st->mQl, st->mKt, a);
+  a.n_tiles = a.n_qt * a.n_rt;
+  const int grid = std::min(a.n_tiles, ctx->sm_count);
+  tc_mstep_kernel<<<grid, ms::THREADS, ms::SMEM_BYTES, ctx->stream>>>(st->mQh, st->mQl, st->mKt, a);
   if ((rc = after_launch(ctx, "tc_mstep_kernel"))) return rc;
   return check_status(p, "tensor-core iteration");
 }

@@ -277,14 +277,19 @@ int emc_plan_bind(emc_plan* plan, const float* d_images, const int* d_mask, cons
  * stats (host, may be NULL) is filled after a synchronise. */
 int emc_iterate(emc_plan* plan, float* d_model, float* d_weight, float sigma,
                 emc_iter_stats* stats);
-/* Tuning of the tensor-core kernels (the autotuner's knobs).
- * EMC_OPT_ESTEP_CLUSTER: CTAs per thread-block cluster of the E-step (1, 2,
- * 4); the cluster shares rotation-side tiles through TMA multicast. */
-#define EMC_OPT_ESTEP_CLUSTER 1
+/* Precision knobs of the tensor-core kernels.
+ * EMC_OPT_ESTEP_GHLO: 1 (default) takes the likelihood's rotation-side
+ * factors s/(s+c) and 1/(s+c) as FP16 hi + lo, 0 as FP16 hi only (4 instead
+ * of 6 MMAs per 16-pixel step, ~2^-12 relative rounding per factor). */
+#define EMC_OPT_ESTEP_GHLO 3
 /* EMC_OPT_MSTEP_QLO: 1 (default) multiplies responsibility/scaling as FP16
  * hi + lo, 0 as FP16 hi only (half the M-step MMAs, ~2^-12 relative
  * rounding per term). */
 #define EMC_OPT_MSTEP_QLO 2
+/* EMC_OPT_MSTEP_AGGREGATE: 1 combines, inside each warp, the nearest-voxel
+ * insertions that land on the same voxel before one atomic (float atomics
+ * only); 0 (default) issues one atomic per rotation-pixel pair. */
+#define EMC_OPT_MSTEP_AGGREGATE 4
 int emc_plan_set_option(emc_plan* plan, int option, int value);
 /* Instrumentation: with profiling on, emc_iterate records CUDA events on the
  * context stream between its phases; emc_plan_phase_ms (after the iteration

@@ -42,14 +42,17 @@ def oracle_run(prob):
     return models, lls
 
 
-@pytest.mark.parametrize("precision,q_lo", [(E.PREC_FP32, 1), (E.PREC_MIXED, 1), (E.PREC_MIXED, 0)],
-                         ids=["fp32", "mixed", "mixed-qhi"])
-def test_mid_geometry_accuracy(ctx, cuda, prob, oracle_run, precision, q_lo):
+@pytest.mark.parametrize("precision,q_lo,gh_lo",
+                         [(E.PREC_FP32, 1, 1), (E.PREC_MIXED, 1, 1), (E.PREC_MIXED, 0, 1),
+                          (E.PREC_MIXED, 0, 0)],
+                         ids=["fp32", "mixed", "mixed-qhi", "mixed-hi"])
+def test_mid_geometry_accuracy(ctx, cuda, prob, oracle_run, precision, q_lo, gh_lo):
     want_models, want_lls = oracle_run
     s, R, N = prob.cfg.side, prob.quats.shape[0], prob.images.shape[0]
     T = lambda a, dt=torch.float32: torch.as_tensor(np.ascontiguousarray(a), dtype=dt, device=cuda)
     plan = E.Plan(ctx, s, N, R, precision=precision)
     plan.set_option(E.Plan.OPT_MSTEP_QLO, q_lo)
+    plan.set_option(E.Plan.OPT_ESTEP_GHLO, gh_lo)
     plan.bind(T(prob.images), T(prob.mask, torch.int32), T(prob.x), T(prob.y), T(prob.z),
               T(prob.quats), T(prob.weights))
     m = T(prob.init_model)
@@ -60,7 +63,7 @@ def test_mid_geometry_accuracy(ctx, cuda, prob, oracle_run, precision, q_lo):
         want = want_models[it]
         rel = np.linalg.norm(got - want) / np.linalg.norm(want)
         ll_rel = abs(st.total_loglik - want_lls[it]) / abs(want_lls[it])
-        print(f"precision {precision} q_lo {q_lo} iteration {it}: model rel L2 {rel:.3e}, LL rel {ll_rel:.3e}")
+        print(f"precision {precision} q_lo {q_lo} gh_lo {gh_lo} iteration {it}: model rel L2 {rel:.3e}, LL rel {ll_rel:.3e}")
         assert rel < 1e-3
         assert ll_rel < 1e-4
     plan.close()

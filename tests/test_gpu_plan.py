@@ -18,9 +18,11 @@ def T(a, dev, dt=torch.float32):
     return torch.as_tensor(np.ascontiguousarray(a), dtype=dt, device=dev)
 
 
-def run_plan(ctx, prob, dev, model=None, sigma=0.3, **kw):
+def run_plan(ctx, prob, dev, model=None, sigma=0.3, options=None, **kw):
     s, R, N = prob.cfg.side, prob.quats.shape[0], prob.images.shape[0]
     plan = E.Plan(ctx, s, N, R, **kw)
+    for opt, val in (options or {}).items():
+        plan.set_option(opt, val)
     plan.bind(T(prob.images, dev), T(prob.mask, dev, torch.int32), T(prob.x, dev), T(prob.y, dev),
               T(prob.z, dev), T(prob.quats, dev), T(prob.weights, dev))
     m = T(prob.init_model if model is None else model, dev)
@@ -60,6 +62,15 @@ MIXED_CASES = [
     (dict(interp=E.INTERP_NEAREST, normalize_images=1), True),
     (dict(interp=E.INTERP_NEAREST, known_intensity=1), False),
     (dict(interp=E.INTERP_NEAREST, insert_mode=E.INSERT_DETERMINISTIC), True),
+    (dict(diff=E.DIFF_TRUE_POISSON, interp=E.INTERP_NEAREST), False),
+    (dict(diff=E.DIFF_TRUE_POISSON, interp=E.INTERP_TRILINEAR), False),
+    (dict(diff=E.DIFF_TRUE_POISSON, interp=E.INTERP_NEAREST, known_intensity=1), False),
+    (dict(diff=E.DIFF_TRUE_POISSON, interp=E.INTERP_NEAREST, normalize_images=1), False),
+    # warp-aggregated insertion atomics
+    (dict(interp=E.INTERP_NEAREST, options={E.Plan.OPT_MSTEP_AGGREGATE: 1}), True),
+    # FP16 hi-only rotation-side factors and M-step operand
+    (dict(interp=E.INTERP_NEAREST, options={E.Plan.OPT_ESTEP_GHLO: 0, E.Plan.OPT_MSTEP_QLO: 0}),
+     True),
 ]
 # tolerances: (log-likelihood rel, scaling rel, model rel L2, respons abs)
 TOL = {E.PREC_FP32: (1e-5, 1e-5, 1e-4, 1e-4), E.PREC_MIXED: (2e-5, 5e-4, 5e-4, 1e-3)}
@@ -115,7 +126,10 @@ def check_against_oracle(ctx, cuda, prob, kw, wellcond, precision):
 
 
 def case_id(c):
-    return "-".join(f"{a}{b}" for a, b in c[0].items())
+    names = {E.Plan.OPT_MSTEP_AGGREGATE: "aggregate", E.Plan.OPT_ESTEP_GHLO: "ghlo",
+             E.Plan.OPT_MSTEP_QLO: "qlo"}
+    return "-".join(f"{a}{b}" if a != "options" else
+                    "-".join(f"{names[o]}{v}" for o, v in b.items()) for a, b in c[0].items())
 
 
 @pytest.mark.parametrize("case", CASES, ids=case_id)

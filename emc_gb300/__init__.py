@@ -276,6 +276,27 @@ class Plan:
                                               C.byref(st) if stats else None), "iterate")
         return st if stats else None
 
+    def iterate_async(self, model, weight, sigma):
+        """Enqueue one iteration; errors and stats come from wait()."""
+        self.ctx._check(self._lib.emc_iterate_async(self._h, _ptr(model), _ptr(weight),
+                                                    float(sigma)), "iterate_async")
+
+    def wait(self, stats: bool = True):
+        st = IterStats()
+        self.ctx._check(self._lib.emc_plan_wait(self._h, C.byref(st) if stats else None),
+                        "plan_wait")
+        return st if stats else None
+
+    def capture(self, model, weight):
+        """Record one iteration on (model, weight) into a CUDA graph."""
+        self._captured = (model, weight)  # keep alive
+        self.ctx._check(self._lib.emc_plan_capture(self._h, _ptr(model), _ptr(weight)),
+                        "plan_capture")
+
+    def replay(self, sigma):
+        """One iteration in place on the captured buffers (asynchronous)."""
+        self.ctx._check(self._lib.emc_plan_replay(self._h, float(sigma)), "plan_replay")
+
     PHASES = ("expand", "estep", "lse", "mprep", "mstep", "finish")
     OPT_ESTEP_GHLO = 3
     OPT_MSTEP_QLO = 2

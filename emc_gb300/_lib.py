@@ -110,6 +110,10 @@ SIGNATURES: dict[str, tuple] = {
     "emc_plan_workspace_bytes": (C.c_size_t, [P]),
     "emc_plan_bind": (I, [P, P, P, P, P, P, P, P]),
     "emc_iterate": (I, [P, P, P, F, C.POINTER(IterStats)]),
+    "emc_iterate_async": (I, [P, P, P, F]),
+    "emc_plan_wait": (I, [P, C.POINTER(IterStats)]),
+    "emc_plan_capture": (I, [P, P, P]),
+    "emc_plan_replay": (I, [P, F]),
     "emc_plan_results": (I, [P, C.POINTER(P), C.POINTER(P), C.POINTER(P)]),
     "emc_plan_set_profiling": (I, [P, I]),
     "emc_plan_set_option": (I, [P, I, I]),

@@ -264,7 +264,7 @@ struct EstepArgs {
   float2* part;        // [n_rt][N]
   int* bad;            // invalid pair counter
   int R, N, Kp;
-  float inv2s2;        // 1 / (2 sigma^2)
+  const float* sigma;  // [1] annealing width (device memory)
   int known_intensity;
 };
 
@@ -441,7 +441,8 @@ __global__ void __launch_bounds__(TPB, 1) estep_fp32_kernel(EstepArgs a) {
     const bool rok = r < a.R;
     const float cnt = rok ? __ldg(a.rot_cnt + r) : 0.0f;
     const float lw = rok ? logf(__ldg(a.rotw + r)) : 0.0f;
-    const float scale = cnt > 0.0f ? a.inv2s2 / cnt : 0.0f;
+    const float sg = *a.sigma;
+    const float scale = cnt > 0.0f ? (1.0f / (2.0f * sg * sg)) / cnt : 0.0f;
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
       const int n = n0 + micro_idx(tx4, j);
@@ -525,10 +526,12 @@ __global__ void __launch_bounds__(TPB, 1) estep_pois_fp32_kernel(EstepArgs a) {
 }
 
 // ------------------------------------------------------- normalise -------
-// lse_i = M + log(sum_t s_t exp(m_t - M)) over the rotation tiles, FP64.
-// Patterns with no valid pair get lse = +inf (all responsibilities 0).
+// lse_i = M + log(sum_t s_t exp(m_t - M)) over the rotation tiles, FP64,
+// also as two floats hi + lo (hi = fl(lse), lo = fl(lse - hi)) so that
+// consumers form L - lse in FP32 to the same accuracy.  Patterns with no
+// valid pair get lse = +inf (all responsibilities 0).
 __global__ void lse_combine_kernel(const float2* __restrict__ part, int n_rt, int N,
-                                   double* __restrict__ lse) {
+                                   double* __restrict__ lse, float2* __restrict__ lse2) {
   const int n = blockIdx.x * blockDim.x + threadIdx.x;
   if (n >= N) return;
   float M = -INFINITY;
@@ -543,6 +546,8 @@ __global__ void lse_combine_kernel(const float2* __restrict__ part, int n_rt, in
     l = (double)M + log(s);
   }
   lse[n] = l;
+  const float hi = (float)l;
+  lse2[n] = make_float2(hi, isfinite(l) ? (float)(l - (double)hi) : 0.0f);
 }
 
 // Deterministic FP64 sum of the finite entries of x[0..n) into out[0]
@@ -571,20 +576,24 @@ __global__ void finite_sum_kernel(const double* __restrict__ x, int n, double* _
 //   the tensor M-step multiplies raw counts) as FP16 hi + lo [R][ldq], each
 //   row scaled by 2^e_r so its largest entry sits near 2^14 (qscale_r =
 //   2^-e_r); the second pass re-reads the row while it is in L2.
-__global__ void __launch_bounds__(256) mprep_kernel(
-    float* __restrict__ L, const float* __restrict__ PHI, const double* __restrict__ lse,
+constexpr int kMprepThreads = 1024;
+constexpr int kMprepStageMax = 30720;  // patterns whose row of Q fits shared memory (120 KB)
+
+__global__ void __launch_bounds__(kMprepThreads) mprep_kernel(
+    float* __restrict__ L, const float* __restrict__ PHI, const float2* __restrict__ lse2,
     const float* __restrict__ Ksum, const float* __restrict__ cnorm, int R, int N,
     float* __restrict__ Q, __half* __restrict__ Qh, __half* __restrict__ Ql,
     float* __restrict__ qscale, int ldq, float* __restrict__ T, double* __restrict__ row_mass,
-    double* __restrict__ row_bound) {
+    double* __restrict__ row_bound, int stage) {
+  extern __shared__ float qrow[];  // [N] when stage: the row's P c_i / phi
   const int r = blockIdx.x;
   float t = 0.0f, b = 0.0f, qmax = 0.0f;
   for (int i = threadIdx.x; i < N; i += blockDim.x) {
     const size_t e = (size_t)r * N + i;
-    const double li = lse[i];
+    const float2 li = lse2[i];
     const float l = L[e];
     float P = 0.0f;
-    if (isfinite(li) && l > -INFINITY) P = expf((float)((double)l - li));
+    if (isfinite(li.x) && l > -INFINITY) P = expf((l - li.x) - li.y);
     L[e] = P;
     const float f = PHI[e];
     float q = f > 0.0f ? __fdiv_rn(P, f) : 0.0f;
@@ -593,11 +602,12 @@ __global__ void __launch_bounds__(256) mprep_kernel(
     if (Qh) q = __fmul_rn(q, __ldg(cnorm + i));
     qmax = fmaxf(qmax, q);
     if (Q) Q[(size_t)r * ldq + i] = q;
+    if (stage) qrow[i] = q;
   }
   if (Q)
     for (int i = N + threadIdx.x; i < ldq; i += blockDim.x) Q[(size_t)r * ldq + i] = 0.0f;
-  __shared__ double sh[2][256];
-  __shared__ float smx[256];
+  __shared__ double sh[2][kMprepThreads];
+  __shared__ float smx[kMprepThreads];
   sh[0][threadIdx.x] = (double)t;
   sh[1][threadIdx.x] = (double)b;
   smx[threadIdx.x] = qmax;
@@ -623,9 +633,13 @@ __global__ void __launch_bounds__(256) mprep_kernel(
   for (int i = threadIdx.x; i < ldq; i += blockDim.x) {
     float q = 0.0f;
     if (i < N) {
-      const size_t e = (size_t)r * N + i;
-      const float f = PHI[e];
-      q = f > 0.0f ? __fmul_rn(__fmul_rn(__fdiv_rn(L[e], f), __ldg(cnorm + i)), up) : 0.0f;
+      if (stage) {
+        q = __fmul_rn(qrow[i], up);
+      } else {  // re-read the row (L now holds P)
+        const size_t e = (size_t)r * N + i;
+        const float f = PHI[e];
+        q = f > 0.0f ? __fmul_rn(__fmul_rn(__fdiv_rn(L[e], f), __ldg(cnorm + i)), up) : 0.0f;
+      }
     }
     const __half hi = __float2half_rn(q);
     Qh[(size_t)r * ldq + i] = hi;
@@ -875,6 +889,12 @@ extern "C" int emc_plan_create(emc_ctx* ctx, const emc_plan_desc* desc, emc_plan
   if (!rc) rc = alloc_n(p, &p->PHI, RN);
   if (!rc) rc = alloc_n(p, &p->part, (size_t)p->n_rt * d.n_images);
   if (!rc) rc = alloc_n(p, &p->lse, d.n_images);
+  if (!rc) rc = alloc_n(p, &p->lse2, d.n_images);
+  if (!rc) {
+    cudaError_t e = cudaFuncSetAttribute(mprep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)(sizeof(float) * kMprepStageMax));
+    if (e != cudaSuccess) rc = cuda_fail(ctx, e, "plan_create: mprep smem");
+  }
   if (!rc) rc = alloc_n(p, &p->T, p->Rp);
   if (!rc) rc = alloc_n(p, &p->rot_cnt, p->Rp);
   if (!rc) rc = alloc_n(p, &p->rot_A, p->Rp);
@@ -883,6 +903,21 @@ extern "C" int emc_plan_create(emc_ctx* ctx, const emc_plan_desc* desc, emc_plan
   if (!rc) rc = alloc_n(p, &p->cnorm, d.n_images);
   if (!rc) rc = alloc_n(p, &p->Ksum, d.n_images);
   if (!rc) rc = alloc_n(p, &p->flags, 16);
+  if (!rc) rc = alloc_n(p, &p->sigma_dev, 1);
+  if (!rc && d.blur_sigma > 0.0f) {
+    const size_t n3b = (size_t)d.side * d.side * d.side;
+    float *ba = nullptr, *bb = nullptr, *bg = nullptr;
+    unsigned char* bk = nullptr;
+    rc = alloc_n(p, &ba, n3b);
+    if (!rc) rc = alloc_n(p, &bb, n3b);
+    if (!rc) rc = alloc_n(p, &bg, (size_t)d.side);
+    if (!rc) rc = plan_alloc(p, (void**)&bk, n3b);
+    if (!rc) rc = blur_prepare(ctx, d.side, d.blur_sigma, ba, bb, bg, bk, &p->blur);
+  }
+  if (!rc) {
+    cudaError_t e = cudaMemsetAsync(p->flags, 0, 16 * sizeof(int), ctx->stream);
+    if (e != cudaSuccess) rc = cuda_fail(ctx, e, "plan_create");
+  }
   if (!rc && d.precision == EMC_PREC_FP32) rc = alloc_n(p, &p->Q, (size_t)d.n_rot * p->Np);
   if (!rc && d.insert_mode == EMC_INSERT_DETERMINISTIC) {
     rc = alloc_n(p, &p->fix_m, n3);
@@ -900,6 +935,8 @@ extern "C" int emc_plan_create(emc_ctx* ctx, const emc_plan_desc* desc, emc_plan
 extern "C" int emc_plan_destroy(emc_plan* p) {
   if (!p) return EMC_OK;
   if (p->ctx) cudaStreamSynchronize(p->ctx->stream);
+  if (p->graph_exec) cudaGraphExecDestroy(p->graph_exec);
+  if (p->graph) cudaGraphDestroy(p->graph);
   for (auto& e : p->ev)
     if (e) cudaEventDestroy(e);
   if (p->tc) tc_free(p);
@@ -1011,7 +1048,7 @@ static int plan_expand(emc_plan* p, const float* model) {
   return after_launch(ctx, "slice_rows_kernel");
 }
 
-static int plan_estep_fp32(emc_plan* p, float sigma) {
+static int plan_estep_fp32(emc_plan* p) {
   emc_ctx* ctx = p->ctx;
   EstepArgs a;
   a.S = p->S;
@@ -1029,7 +1066,7 @@ static int plan_estep_fp32(emc_plan* p, float sigma) {
   a.R = p->d.n_rot;
   a.N = p->d.n_images;
   a.Kp = p->Kp;
-  a.inv2s2 = 1.0f / (2.0f * sigma * sigma);
+  a.sigma = p->sigma_dev;
   a.known_intensity = p->d.known_intensity;
   dim3 grid(ceil_div(a.N, BN), ceil_div(a.R, BM));
   if (p->d.diff == EMC_DIFF_POISSON)
@@ -1077,13 +1114,12 @@ static int plan_mstep_fp32(emc_plan* p, float* model, float* weight, const Inser
   return after_launch(ctx, "mstep_fp32_kernel");
 }
 
-extern "C" int emc_iterate(emc_plan* p, float* d_model, float* d_weight, float sigma,
-                           emc_iter_stats* stats) {
-  if (!p) return EMC_ERR_INVALID;
+// Enqueues one iteration on the context stream: kernels, device-to-device
+// copies and memsets only (no allocation, no host copy, no synchronisation),
+// so the sequence can be captured in a CUDA graph.  The E-step reads sigma
+// from p->sigma_dev.
+static int iterate_enqueue(emc_plan* p, float* d_model, float* d_weight) {
   emc_ctx* ctx = p->ctx;
-  EMC_REQUIRE(ctx, p->bound, "iterate: plan not bound");
-  EMC_REQUIRE(ctx, d_model && d_weight, "iterate: null model/weight");
-  EMC_REQUIRE(ctx, sigma > 0.0f && std::isfinite(sigma), "iterate: bad sigma");
   const int R = p->d.n_rot, N = p->d.n_images;
   const long long n3 = (long long)p->d.side * p->d.side * p->d.side;
   int rc;
@@ -1098,13 +1134,14 @@ extern "C" int emc_iterate(emc_plan* p, float* d_model, float* d_weight, float s
   if ((rc = mark(1))) return rc;
   // scaling + likelihood + per-tile LSE partials
   if (p->d.precision == EMC_PREC_MIXED)
-    rc = tc_estep(p, sigma);
+    rc = tc_estep(p);
   else
-    rc = plan_estep_fp32(p, sigma);
+    rc = plan_estep_fp32(p);
   if (rc) return rc;
   if ((rc = mark(2))) return rc;
   // normaliser
-  lse_combine_kernel<<<ceil_div(N, 256), 256, 0, ctx->stream>>>(p->part, p->n_rt, N, p->lse);
+  lse_combine_kernel<<<ceil_div(N, 256), 256, 0, ctx->stream>>>(p->part, p->n_rt, N, p->lse,
+                                                                p->lse2);
   if ((rc = after_launch(ctx, "lse_combine_kernel"))) return rc;
   finite_sum_kernel<<<1, 256, 0, ctx->stream>>>(p->lse, N, p->red + kRedLL);
   if ((rc = after_launch(ctx, "finite_sum_kernel"))) return rc;
@@ -1112,10 +1149,11 @@ extern "C" int emc_iterate(emc_plan* p, float* d_model, float* d_weight, float s
   double* row_mass = p->red + kRedSlots;
   double* row_bound = row_mass + p->Rp;
   const bool tcm = p->d.precision == EMC_PREC_MIXED;
-  mprep_kernel<<<R, 256, 0, ctx->stream>>>(p->L, p->PHI, p->lse, p->Ksum, p->cnorm, R, N,
-                                            tcm ? nullptr : p->Q, tcm ? p->Qh : nullptr,
-                                            tcm ? p->Ql : nullptr, p->qscale, p->Np, p->T,
-                                            row_mass, row_bound);
+  const int stage = tcm && N <= kMprepStageMax;
+  mprep_kernel<<<R, kMprepThreads, stage ? sizeof(float) * N : 0, ctx->stream>>>(
+      p->L, p->PHI, p->lse2, p->Ksum, p->cnorm, R, N, tcm ? nullptr : p->Q,
+      tcm ? p->Qh : nullptr, tcm ? p->Ql : nullptr, p->qscale, p->Np, p->T, row_mass, row_bound,
+      stage);
   if ((rc = after_launch(ctx, "mprep_kernel"))) return rc;
   if ((rc = mark(4))) return rc;
   // M-step into zeroed accumulators
@@ -1152,27 +1190,122 @@ extern "C" int emc_iterate(emc_plan* p, float* d_model, float* d_weight, float s
                                 ctx->stream));
   if ((rc = launch_scale_by_inverse_mean(ctx, d_model, n3, tail))) return rc;
   if (p->d.blur_sigma > 0.0f) {
-    if ((rc = launch_blur(ctx, d_model, p->d.side, p->d.blur_sigma))) return rc;
+    if ((rc = blur_run(ctx, d_model, p->blur))) return rc;
   }
-  if ((rc = mark(6))) return rc;
+  return mark(6);
+}
+
+static int set_sigma(emc_plan* p, float sigma) {
+  emc_ctx* ctx = p->ctx;
+  EMC_REQUIRE(ctx, sigma > 0.0f && std::isfinite(sigma), "iterate: bad sigma");
+  // pageable source: staged before the call returns, ordered on the stream
+  EMC_CUDA(ctx, cudaMemcpyAsync(p->sigma_dev, &sigma, sizeof(float), cudaMemcpyHostToDevice,
+                                ctx->stream));
+  return EMC_OK;
+}
+
+extern "C" int emc_iterate_async(emc_plan* p, float* d_model, float* d_weight, float sigma) {
+  if (!p) return EMC_ERR_INVALID;
+  emc_ctx* ctx = p->ctx;
+  EMC_REQUIRE(ctx, p->bound, "iterate: plan not bound");
+  EMC_REQUIRE(ctx, d_model && d_weight, "iterate: null model/weight");
+  int rc = set_sigma(p, sigma);
+  if (rc) return rc;
+  return iterate_enqueue(p, d_model, d_weight);
+}
+
+// Synchronises, then reports what the device recorded since the last wait:
+// a pipeline wait that timed out, slice values outside the FP16 operand
+// range; fills stats (of the last iteration) and clears the status words.
+extern "C" int emc_plan_wait(emc_plan* p, emc_iter_stats* stats) {
+  if (!p) return EMC_ERR_INVALID;
+  emc_ctx* ctx = p->ctx;
+  const int R = p->d.n_rot, N = p->d.n_images;
+  int hflags[8] = {0};
+  int tcs = 0;
+  int* dtc = tc_status(p);
+  double h[kRedSlots];
+  std::vector<double> mass(stats ? R : 0);
+  EMC_CUDA(ctx, cudaMemcpyAsync(hflags, p->flags, sizeof(hflags), cudaMemcpyDeviceToHost,
+                                ctx->stream));
+  if (dtc)
+    EMC_CUDA(ctx, cudaMemcpyAsync(&tcs, dtc, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
   if (stats) {
-    double h[kRedSlots];
-    int bad = 0;
-    std::vector<double> mass(R);
     EMC_CUDA(ctx, cudaMemcpyAsync(h, p->red, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
-    EMC_CUDA(ctx, cudaMemcpyAsync(mass.data(), row_mass, sizeof(double) * R,
+    EMC_CUDA(ctx, cudaMemcpyAsync(mass.data(), p->red + kRedSlots, sizeof(double) * R,
                                   cudaMemcpyDeviceToHost, ctx->stream));
-    EMC_CUDA(ctx, cudaMemcpyAsync(&bad, p->flags + 4, sizeof(int), cudaMemcpyDeviceToHost,
-                                  ctx->stream));
-    EMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  }
+  EMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  if (dtc && tcs) EMC_CUDA(ctx, cudaMemsetAsync(dtc, 0, sizeof(int), ctx->stream));
+  if (hflags[0] & 4) EMC_CUDA(ctx, cudaMemsetAsync(p->flags, 0, sizeof(int), ctx->stream));
+  if (tcs)
+    return fail(ctx, EMC_ERR_TIMEOUT, "iterate: tensor-core pipeline wait timed out (status 0x%x)",
+                tcs);
+  if (hflags[0] & 4)
+    return fail(ctx, EMC_ERR_UNSUPPORTED, "iterate: slice values exceed the FP16 operand range");
+  if (stats) {
     double m = 0.0;
     for (double v : mass) m += v;
     stats->total_loglik = h[kRedLL];
     stats->model_mean_before = h[kRedMean + 1] > 0 ? h[kRedMean] / h[kRedMean + 1] : 0.0;
     stats->captured_mass = m / (double)N;
-    stats->bad_pairs = bad;
+    stats->bad_pairs = hflags[4];
     stats->reserved = 0;
   }
+  return EMC_OK;
+}
+
+extern "C" int emc_iterate(emc_plan* p, float* d_model, float* d_weight, float sigma,
+                           emc_iter_stats* stats) {
+  int rc = emc_iterate_async(p, d_model, d_weight, sigma);
+  if (rc) return rc;
+  return emc_plan_wait(p, stats);
+}
+
+extern "C" int emc_plan_capture(emc_plan* p, float* d_model, float* d_weight) {
+  if (!p) return EMC_ERR_INVALID;
+  emc_ctx* ctx = p->ctx;
+  EMC_REQUIRE(ctx, p->bound, "plan_capture: plan not bound");
+  EMC_REQUIRE(ctx, d_model && d_weight, "plan_capture: null model/weight");
+  EMC_REQUIRE(ctx, ctx->stream != nullptr,
+              "plan_capture: the legacy default stream cannot be captured; use emc_set_stream");
+  if (p->graph_exec) {
+    EMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    cudaGraphExecDestroy(p->graph_exec);
+    p->graph_exec = nullptr;
+  }
+  if (p->graph) {
+    cudaGraphDestroy(p->graph);
+    p->graph = nullptr;
+  }
+  const bool prof = p->profiling;
+  p->profiling = false;  // no event records inside the graph
+  EMC_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+  const int rc = iterate_enqueue(p, d_model, d_weight);
+  cudaGraph_t g = nullptr;
+  const cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+  p->profiling = prof;
+  if (rc) {
+    if (g) cudaGraphDestroy(g);
+    return rc;
+  }
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "plan_capture: end capture");
+  const cudaError_t ei = cudaGraphInstantiate(&p->graph_exec, g, 0);
+  if (ei != cudaSuccess) {
+    cudaGraphDestroy(g);
+    return cuda_fail(ctx, ei, "plan_capture: instantiate");
+  }
+  p->graph = g;
+  return EMC_OK;
+}
+
+extern "C" int emc_plan_replay(emc_plan* p, float sigma) {
+  if (!p) return EMC_ERR_INVALID;
+  emc_ctx* ctx = p->ctx;
+  EMC_REQUIRE(ctx, p->graph_exec, "plan_replay: no captured iteration");
+  int rc = set_sigma(p, sigma);
+  if (rc) return rc;
+  EMC_CUDA(ctx, cudaGraphLaunch(p->graph_exec, ctx->stream));
   return EMC_OK;
 }
 

@@ -18,6 +18,20 @@ int launch_divide_by_weight(emc_ctx* ctx, float* model, const float* weight, lon
 
 int launch_blur(emc_ctx* ctx, float* model, int side, float sigma);
 
+// Blur in two halves: blur_prepare uploads the taps into caller-owned device
+// buffers (a, b: side^3 floats, g: side floats, keep: side^3 bytes) once;
+// blur_run enqueues the passes without allocating or copying from the host,
+// so it can be captured in a CUDA graph.
+struct BlurWork {
+  float *a, *b, *g;
+  unsigned char* keep;
+  int side, h_lo, h_hi;
+};
+size_t blur_work_bytes(int side);
+int blur_prepare(emc_ctx* ctx, int side, float sigma, float* a, float* b, float* g,
+                 unsigned char* keep, BlurWork* w);
+int blur_run(emc_ctx* ctx, float* model, const BlurWork& w);
+
 // Nearest-voxel insertion with the reference's bounds (emc_atomic.cu:33-85).
 int launch_insert_nearest(emc_ctx* ctx, const float* slices, const int* mask, const float* totals,
                           const float* rot, const float* x, const float* y, const float* z,

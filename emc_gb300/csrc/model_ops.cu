@@ -238,38 +238,67 @@ static BlurTaps blur_taps(int side, double sigma, std::vector<float>& g) {
   return t;
 }
 
-int launch_blur(emc_ctx* ctx, float* model, int side, float sigma) {
-  const long long n3 = (long long)side * side * side;
-  const size_t bytes = sizeof(float) * (2 * n3 + side) + n3 + 256;
-  int rc = ensure_scratch(ctx, bytes);
-  if (rc) return rc;
-  float* a = (float*)ctx->scratch;
-  float* b = a + n3;
-  float* g = b + n3;
-  unsigned char* keep = (unsigned char*)(g + side);
+int blur_prepare(emc_ctx* ctx, int side, float sigma, float* a, float* b, float* g,
+                 unsigned char* keep, BlurWork* w) {
   std::vector<float> taps;
-  BlurTaps t = blur_taps(side, (double)sigma, taps);
+  const BlurTaps t = blur_taps(side, (double)sigma, taps);
   // Pageable source: the call returns once `taps` has been staged.
   EMC_CUDA(ctx, cudaMemcpyAsync(g, taps.data(), sizeof(float) * side, cudaMemcpyHostToDevice,
                                 ctx->stream));
-  const int rthreads = std::min(256, ((side + 31) / 32) * 32);
-  blur_rows_kernel<<<side * side, rthreads, sizeof(float) * side, ctx->stream>>>(model, a, keep, g,
-                                                                                 side, t, 1);
-  if ((rc = after_launch(ctx, "blur_rows_kernel"))) return rc;
   const size_t csm = sizeof(float) * side * 33;
   if (csm > 48 * 1024) {
     EMC_CUDA(ctx, cudaFuncSetAttribute(blur_cols_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)csm));
   }
+  w->a = a;
+  w->b = b;
+  w->g = g;
+  w->keep = keep;
+  w->side = side;
+  w->h_lo = t.h_lo;
+  w->h_hi = t.h_hi;
+  return EMC_OK;
+}
+
+size_t blur_work_bytes(int side) {
+  const long long n3 = (long long)side * side * side;
+  return sizeof(float) * (2 * n3 + side) + n3 + 256;
+}
+
+// Enqueues the three passes only: no allocation, no host copy (capturable).
+int blur_run(emc_ctx* ctx, float* model, const BlurWork& w) {
+  const int side = w.side;
+  BlurTaps t;
+  t.h_lo = w.h_lo;
+  t.h_hi = w.h_hi;
+  int rc;
+  const int rthreads = std::min(256, ((side + 31) / 32) * 32);
+  blur_rows_kernel<<<side * side, rthreads, sizeof(float) * side, ctx->stream>>>(
+      model, w.a, w.keep, w.g, side, t, 1);
+  if ((rc = after_launch(ctx, "blur_rows_kernel"))) return rc;
+  const size_t csm = sizeof(float) * side * 33;
   dim3 grid(ceil_div(side, 32), side);
   // y pass: lines along y, bundles indexed by z.
-  blur_cols_kernel<<<grid, 256, csm, ctx->stream>>>(a, b, keep, g, side, side,
+  blur_cols_kernel<<<grid, 256, csm, ctx->stream>>>(w.a, w.b, w.keep, w.g, side, side,
                                                     (long long)side * side, t, 0);
   if ((rc = after_launch(ctx, "blur_cols_kernel"))) return rc;
   // z pass: lines along z, bundles indexed by y.
-  blur_cols_kernel<<<grid, 256, csm, ctx->stream>>>(b, model, keep, g, side,
+  blur_cols_kernel<<<grid, 256, csm, ctx->stream>>>(w.b, model, w.keep, w.g, side,
                                                     (long long)side * side, side, t, 1);
   return after_launch(ctx, "blur_cols_kernel");
+}
+
+int launch_blur(emc_ctx* ctx, float* model, int side, float sigma) {
+  const long long n3 = (long long)side * side * side;
+  int rc = ensure_scratch(ctx, blur_work_bytes(side));
+  if (rc) return rc;
+  float* a = (float*)ctx->scratch;
+  float* b = a + n3;
+  float* g = b + n3;
+  unsigned char* keep = (unsigned char*)(g + side);
+  BlurWork w;
+  if ((rc = blur_prepare(ctx, side, sigma, a, b, g, keep, &w))) return rc;
+  return blur_run(ctx, model, w);
 }
 
 }  // namespace emc

@@ -6,6 +6,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "kernels.cuh"
 
 // Rotations per E-step tile; LSE partials are kept per tile of this many rows.
 #define EMC_RT 128
@@ -62,12 +63,19 @@ struct emc_plan {
   float* qscale = nullptr; // [Rp] 2^-e_r of the Q rows
   float2* part = nullptr;  // [n_rt][N] (max, sumexp) per rotation tile
   double* lse = nullptr;   // [N]
+  float2* lse2 = nullptr;  // [N] lse as float hi + lo
   float* T = nullptr;      // [Rp] rotation totals
   double* red = nullptr;   // reduction scratch (small)
   unsigned long long* fix_m = nullptr;  // [s^3] fixed-point model (deterministic insert)
   unsigned long long* fix_w = nullptr;
   float2* acc2 = nullptr;  // [s^3] interleaved (model, weight) sums (float atomics)
   int* flags = nullptr;    // device status words
+  float* sigma_dev = nullptr;  // [1] annealing width read by the E-step kernels
+  emc::BlurWork blur{};        // plan-owned blur buffers and taps (blur_sigma > 0)
+
+  // one captured iteration (emc_plan_capture / emc_plan_replay)
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t graph_exec = nullptr;
 
   // per-phase CUDA events on the context stream (emc_plan_set_profiling)
   static constexpr int kPhases = 6;  // expand, estep, lse, mprep, mstep, finish
@@ -100,8 +108,9 @@ int plan_alloc(emc_plan* p, void** ptr, size_t bytes);
 
 // Tensor-core path (tc_gemm.cu).
 int tc_bind(emc_plan* p);
-int tc_estep(emc_plan* p, float sigma);
+int tc_estep(emc_plan* p);
 int tc_mstep(emc_plan* p, float* model, float* weight);
+int* tc_status(emc_plan* p);  // device status word of the tensor-core pipelines
 void tc_free(emc_plan* p);
 
 }  // namespace emc

@@ -214,7 +214,7 @@ struct TcEstepArgs {
   const float* rot_A;
   const float* rotw;
   const float* cnorm;   // c_i (phi is stored as c_i num/den)
-  float inv2s2;         // 1 / (2 sigma^2)
+  const float* sigma;   // [1] annealing width (device memory)
   int known_intensity;
   float* L;
   float* PHI;
@@ -241,6 +241,8 @@ __global__ void __launch_bounds__(es::THREADS, 1)
   float* s_lw = s_scale + BN;
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const float sg = *a.sigma;
+  const float inv2s2 = 1.0f / (2.0f * sg * sg);
   // grouped raster: GROUP rotation tiles share each pattern tile in turn
   const int per_group = GROUP * a.n_pt;
   const int g = blockIdx.x / per_group, within = blockIdx.x % per_group;
@@ -262,7 +264,7 @@ __global__ void __launch_bounds__(es::THREADS, 1)
     const int r = r0 + threadIdx.x;
     const float cnt = r < a.R ? a.rot_cnt[r] : 0.0f;
     s_A[threadIdx.x] = r < a.R ? a.rot_A[r] : 0.0f;
-    s_scale[threadIdx.x] = cnt > 0.0f ? a.inv2s2 / cnt : -1.0f;  // < 0: invalid rotation
+    s_scale[threadIdx.x] = cnt > 0.0f ? inv2s2 / cnt : -1.0f;  // < 0: invalid rotation
     s_lw[threadIdx.x] = r < a.R ? logf(a.rotw[r]) : 0.0f;
   }
   if (warp == 1) {
@@ -860,6 +862,7 @@ int tc_bind(emc_plan* p) {
     if (!rc) rc = plan_alloc(p, (void**)&p->qscale, (size_t)Rp * 4);
     if (!rc) rc = plan_alloc(p, (void**)&st->status, 64);
     if (rc) return rc;
+    EMC_CUDA(ctx, cudaMemsetAsync(st->status, 0, 64, ctx->stream));
     EMC_CUDA(ctx, cudaMemsetAsync(p->Qh, 0, (size_t)Rp * Np * 2, ctx->stream));
     EMC_CUDA(ctx, cudaMemsetAsync(p->Ql, 0, (size_t)Rp * Np * 2, ctx->stream));
     // tensor maps (fixed addresses for the plan's lifetime)
@@ -895,18 +898,7 @@ int tc_bind(emc_plan* p) {
   return after_launch(ctx, "transpose_h_kernel");
 }
 
-static int check_status(emc_plan* p, const char* what) {
-  emc_ctx* ctx = p->ctx;
-  int h = 0, f = 0;
-  EMC_CUDA(ctx, cudaMemcpyAsync(&h, state(p)->status, sizeof(int), cudaMemcpyDeviceToHost,
-                                ctx->stream));
-  EMC_CUDA(ctx, cudaMemcpyAsync(&f, p->flags, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-  EMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-  if (h) return fail(ctx, EMC_ERR_TIMEOUT, "%s: pipeline wait timed out (status 0x%x)", what, h);
-  if (f & 4)
-    return fail(ctx, EMC_ERR_UNSUPPORTED, "%s: slice values exceed the FP16 operand range", what);
-  return EMC_OK;
-}
+int* tc_status(emc_plan* p) { return p->tc ? state(p)->status : nullptr; }
 
 static int tc_estep_pois(emc_plan* p) {
   emc_ctx* ctx = p->ctx;
@@ -915,7 +907,6 @@ static int tc_estep_pois(emc_plan* p) {
   int rc;
   tc_rot_logs_kernel<<<ctx->sm_count * 8, 256, 0, ctx->stream>>>(p->S, rk, st->Gh, st->Gl);
   if ((rc = after_launch(ctx, "tc_rot_logs_kernel"))) return rc;
-  EMC_CUDA(ctx, cudaMemsetAsync(st->status, 0, sizeof(int), ctx->stream));
   TcEstepPoisArgs a;
   a.N = p->d.n_images;
   a.R = p->d.n_rot;
@@ -937,7 +928,7 @@ static int tc_estep_pois(emc_plan* p) {
   return after_launch(ctx, "tc_estep_pois_kernel");
 }
 
-int tc_estep(emc_plan* p, float sigma) {
+int tc_estep(emc_plan* p) {
   if (p->d.diff == EMC_DIFF_TRUE_POISSON) return tc_estep_pois(p);
   emc_ctx* ctx = p->ctx;
   TcState* st = state(p);
@@ -946,7 +937,6 @@ int tc_estep(emc_plan* p, float sigma) {
   tc_rot_ops_kernel<<<ctx->sm_count * 8, 256, 0, ctx->stream>>>(p->S, rk, st->Mp, st->MSh, st->Gh,
                                                                 st->Gl, st->Hh, st->Hl, p->flags);
   if ((rc = after_launch(ctx, "tc_rot_ops_kernel"))) return rc;
-  EMC_CUDA(ctx, cudaMemsetAsync(st->status, 0, sizeof(int), ctx->stream));
   TcEstepArgs a;
   a.N = p->d.n_images;
   a.R = p->d.n_rot;
@@ -960,7 +950,7 @@ int tc_estep(emc_plan* p, float sigma) {
   a.rot_A = p->rot_A;
   a.rotw = p->rotw;
   a.cnorm = p->cnorm;
-  a.inv2s2 = 1.0f / (2.0f * sigma * sigma);
+  a.sigma = p->sigma_dev;
   a.known_intensity = p->d.known_intensity;
   a.L = p->L;
   a.PHI = p->PHI;
@@ -978,7 +968,6 @@ int tc_estep(emc_plan* p, float sigma) {
 int tc_mstep(emc_plan* p, float* model, float* weight) {
   emc_ctx* ctx = p->ctx;
   TcState* st = state(p);
-  int rc;
   TcMstepArgs a;
   a.R = p->d.n_rot;
   a.Kp = p->Kp;
@@ -1008,8 +997,7 @@ int tc_mstep(emc_plan* p, float* model, float* weight) {
   a.n_tiles = a.n_qt * a.n_rt;
   const int grid = std::min(a.n_tiles, ctx->sm_count);
   tc_mstep_kernel<<<grid, ms::THREADS, ms::SMEM_BYTES, ctx->stream>>>(st->mQh, st->mQl, st->mKt, a);
-  if ((rc = after_launch(ctx, "tc_mstep_kernel"))) return rc;
-  return check_status(p, "tensor-core iteration");
+  return after_launch(ctx, "tc_mstep_kernel");
 }
 
 void tc_free(emc_plan* p) {

@@ -277,6 +277,22 @@ int emc_plan_bind(emc_plan* plan, const float* d_images, const int* d_mask, cons
  * stats (host, may be NULL) is filled after a synchronise. */
 int emc_iterate(emc_plan* plan, float* d_model, float* d_weight, float sigma,
                 emc_iter_stats* stats);
+/* emc_iterate in two halves (replaces the per-iteration body of main.cpp:
+ * 239-480 without its host round trips).  emc_iterate_async only enqueues
+ * the iteration on the context stream and returns; emc_plan_wait
+ * synchronises, reports any device-side failure recorded since the previous
+ * wait (EMC_ERR_TIMEOUT: a bounded pipeline wait gave up; EMC_ERR_UNSUPPORTED:
+ * slice values outside the FP16 operand range) and fills stats (may be NULL)
+ * for the last iteration. */
+int emc_iterate_async(emc_plan* plan, float* d_model, float* d_weight, float sigma);
+int emc_plan_wait(emc_plan* plan, emc_iter_stats* stats);
+/* CUDA-graph form of the iteration.  emc_plan_capture records one iteration
+ * on d_model/d_weight into a graph (the context stream must not be the legacy
+ * default stream); emc_plan_replay(plan, sigma) launches it with a new sigma.
+ * Each replay is one iteration in place on the captured buffers; call
+ * emc_plan_wait for errors and stats.  Re-capture after emc_plan_bind. */
+int emc_plan_capture(emc_plan* plan, float* d_model, float* d_weight);
+int emc_plan_replay(emc_plan* plan, float sigma);
 /* Precision knobs of the tensor-core kernels.
  * EMC_OPT_ESTEP_GHLO: 1 (default) takes the likelihood's rotation-side
  * factors s/(s+c) and 1/(s+c) as FP16 hi + lo, 0 as FP16 hi only (4 instead

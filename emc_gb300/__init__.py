@@ -85,6 +85,15 @@ def sigma_schedule(iteration: int, sigma_start: float, sigma_final: float, half_
     return float(_lib.load().emc_sigma_schedule(iteration, sigma_start, sigma_final, half_life))
 
 
+def random_rotations(seed: int, n: int):
+    """quaternion_random (rotations.c:30-41) n times from a seeded generator: [n, 4] float32."""
+    q = np.zeros((n, 4), np.float32)
+    rc = _lib.load().emc_random_rotations(int(seed), int(n), q.ctypes.data if n else None)
+    if rc != 0:
+        raise EmcError(f"emc_random_rotations failed ({rc})")
+    return q
+
+
 def read_config(path=None, text=None) -> "_lib.Config":
     """emc.conf (configs.cpp:40-90 keys) -> emc_config; raises EmcError on a
     syntax or type error."""
@@ -224,6 +233,40 @@ class Context:
     def blur_model(self, model, side, sigma):
         self._check(self._lib.emc_blur_model(self._h, _ptr(model), side, float(sigma)),
                     "blur_model")
+
+    # -- preprocessing and model initialisation (main.cpp:92-108) -----------
+    def bin_images(self, raw, raw_mask, raw_w, raw_h, n_images, side, stride, images, masks):
+        import torch
+        self._check(self._lib.emc_bin_images(
+            self._h, _ptr(raw, torch.float32, "raw"), _ptr(raw_mask, torch.int32, "raw_mask"),
+            raw_w, raw_h, n_images, side, stride, _ptr(images, torch.float32, "images"),
+            _ptr(masks, torch.int32, "masks")), "bin_images")
+
+    def normalize_images(self, images, mask, n_2d, n_images, masks=None):
+        import torch
+        self._check(self._lib.emc_normalize_images(
+            self._h, _ptr(images, torch.float32, "images"), _ptr(mask, torch.int32, "mask"),
+            _ptr(masks, torch.int32, "masks"), n_2d, n_images), "normalize_images")
+
+    def mask_model(self, images, masks, n_2d, n_images):
+        import torch
+        self._check(self._lib.emc_mask_images(self._h, _ptr(images, torch.float32, "images"),
+                                              _ptr(masks, torch.int32, "masks"), n_2d,
+                                              n_images), "mask_images")
+
+    def model_init_radial(self, images, n_images, side, model):
+        import torch
+        self._check(self._lib.emc_model_init_radial(
+            self._h, _ptr(images, torch.float32, "images"), n_images, side,
+            _ptr(model, torch.float32, "model")), "model_init_radial")
+
+    def model_init_orientations(self, images, mask, n_images, side, rot, x, y, z, model, weight):
+        import torch
+        self._check(self._lib.emc_model_init_orientations(
+            self._h, _ptr(images, torch.float32, "images"), _ptr(mask, torch.int32, "mask"),
+            n_images, side, _ptr(rot, torch.float32, "rot"), _ptr(x), _ptr(y), _ptr(z),
+            _ptr(model, torch.float32, "model"), _ptr(weight, torch.float32, "weight")),
+            "model_init_orientations")
 
     def reset_real(self, x, n=None):
         self._check(self._lib.emc_reset_real(self._h, _ptr(x), n if n is not None else x.numel()),

@@ -111,6 +111,12 @@ SIGNATURES: dict[str, tuple] = {
     "emc_plan_bind": (I, [P, P, P, P, P, P, P, P]),
     "emc_iterate": (I, [P, P, P, F, C.POINTER(IterStats)]),
     "emc_iterate_async": (I, [P, P, P, F]),
+    "emc_random_rotations": (I, [C.c_ulonglong, I, P]),
+    "emc_bin_images": (I, [P, P, P, I, I, I, I, I, P, P]),
+    "emc_normalize_images": (I, [P, P, P, P, I, I]),
+    "emc_mask_images": (I, [P, P, P, I, I]),
+    "emc_model_init_radial": (I, [P, P, I, I, P]),
+    "emc_model_init_orientations": (I, [P, P, P, I, I, P, P, P, P, P, P]),
     "emc_plan_wait": (I, [P, C.POINTER(IterStats)]),
     "emc_plan_capture": (I, [P, P, P]),
     "emc_plan_replay": (I, [P, F]),

@@ -7,11 +7,20 @@
 //
 // config defaults to ../emc.conf as in main.cpp:66-70.  Inputs replace the
 // reference's HDF5 reads (emc_helper.cpp:198-368, absent libraries) by raw
-// little-endian files of already-binned data:
+// little-endian files:
+//   <image_prefix>raw.bin      float32 [N_images][detector_size^2] detector frames and
+//   <image_prefix>raw_mask.bin int32   [N_images][detector_size^2] their masks, binned on
+//                              the GPU by read_stride (emc_bin_images, emc_helper.cpp:226-243)
+//                              into patterns and per-pattern masks; or, when raw.bin is
+//                              absent, already-binned patterns:
 //   <image_prefix>images.bin   float32 [N_images][model_side^2]  (y*side + x)
 //   <mask_file>                int32   [model_side^2]
 //   <model_file>               float32 [model_side^3]            (model_input 2)
-// model_input 0 starts from a seeded uniform [0,1) model (emc_helper.cpp:449-456).
+// Preprocessing follows main.cpp:92-108 on the GPU: binning, normalisation
+// (normalize_images), model_init, then mask_model (-1 at per-pattern masked
+// pixels).  model_input 0 starts from a seeded uniform [0,1) model
+// (emc_helper.cpp:449-456), 1 inserts every pattern at a seeded random
+// orientation (:503-518), 3 is the radial average of the patterns (:458-502).
 // Outputs follow file_helper.cpp:30-127 with raw files instead of HDF5:
 //   output/model_%04d.bin (+ .mask.bin, .json)   value where weight > 0 and
 //                                                model > 0, else 0 with mask 0
@@ -64,6 +73,12 @@ std::vector<T> read_raw(const std::string& path, size_t n) {
   std::fclose(f);
   if (got != n) die("short file", path.c_str());
   return v;
+}
+
+bool file_exists(const std::string& path) {
+  FILE* f = std::fopen(path.c_str(), "rb");
+  if (f) std::fclose(f);
+  return f != nullptr;
 }
 
 template <typename T>
@@ -152,8 +167,10 @@ int main(int argc, char** argv) {
   std::vector<float> x(n2), y(n2), z(n2);
   emc_calculate_coordinates(side, (float)cfg.pixel_size, (float)cfg.detector_distance,
                             (float)cfg.wavelength, x.data(), y.data(), z.data());
-  std::vector<float> images = read_raw<float>(std::string(cfg.image_prefix) + "images.bin",
-                                              (size_t)N * n2);
+  const std::string raw_path = std::string(cfg.image_prefix) + "raw.bin";
+  const bool have_raw = file_exists(raw_path);
+  std::vector<float> images;
+  if (!have_raw) images = read_raw<float>(std::string(cfg.image_prefix) + "images.bin", (size_t)N * n2);
   std::vector<int> mask = read_raw<int>(cfg.mask_file, n2);
   std::vector<float> model(n3);
   if (cfg.model_input == 2) {
@@ -161,8 +178,8 @@ int main(int argc, char** argv) {
   } else if (cfg.model_input == 0) {
     Pcg32 rng;
     for (auto& v : model) v = rng.uniform();
-  } else {
-    die("model_input 1 and 3 are not supported by this driver");
+  } else if (cfg.model_input != 1 && cfg.model_input != 3) {
+    die("model_input must be 0, 1, 2 or 3");
   }
 
   // ---- device
@@ -170,6 +187,7 @@ int main(int argc, char** argv) {
   if (emc_ctx_create(&ctx, 0) != EMC_OK) die("no CUDA device");
   float *d_images, *d_model, *d_weight, *d_x, *d_y, *d_z, *d_rot, *d_w;
   int* d_mask;
+  int* d_masks = nullptr;  // per-pattern masks of the binned frames
   check(emc_allocate_real(ctx, &d_images, (size_t)N * n2), ctx, "alloc");
   check(emc_allocate_real(ctx, &d_model, n3), ctx, "alloc");
   check(emc_allocate_real(ctx, &d_weight, n3), ctx, "alloc");
@@ -179,14 +197,65 @@ int main(int argc, char** argv) {
   check(emc_allocate_real(ctx, &d_rot, 4 * (size_t)R), ctx, "alloc");
   check(emc_allocate_real(ctx, &d_w, R), ctx, "alloc");
   check(emc_allocate_int(ctx, &d_mask, n2), ctx, "alloc");
-  check(emc_copy_real_to_device(ctx, images.data(), d_images, N * n2), ctx, "copy");
-  check(emc_copy_real_to_device(ctx, model.data(), d_model, (int)n3), ctx, "copy");
+  if (have_raw) {  // read_images (emc_helper.cpp:198-245): bin the frames on the GPU
+    const int D = cfg.detector_size;
+    if (D <= 0 || cfg.read_stride <= 0) die("raw frames need detector_size and read_stride > 0");
+    std::vector<float> raw = read_raw<float>(raw_path, (size_t)N * D * D);
+    std::vector<int> raw_mask =
+        read_raw<int>(std::string(cfg.image_prefix) + "raw_mask.bin", (size_t)N * D * D);
+    float* d_raw = nullptr;
+    int* d_raw_mask = nullptr;
+    check(emc_allocate_real(ctx, &d_raw, (size_t)N * D * D), ctx, "alloc");
+    check(emc_allocate_int(ctx, &d_raw_mask, (size_t)N * D * D), ctx, "alloc");
+    check(emc_allocate_int(ctx, &d_masks, (size_t)N * n2), ctx, "alloc");
+    check(emc_copy_real_to_device(ctx, raw.data(), d_raw, N * D * D), ctx, "copy");
+    check(emc_copy_int_to_device(ctx, raw_mask.data(), d_raw_mask, N * D * D), ctx, "copy");
+    for (int i0 = 0; i0 < N; i0 += 65535) {
+      const int c = std::min(65535, N - i0);
+      check(emc_bin_images(ctx, d_raw + (size_t)i0 * D * D, d_raw_mask + (size_t)i0 * D * D, D, D,
+                           c, side, cfg.read_stride, d_images + (size_t)i0 * n2,
+                           d_masks + (size_t)i0 * n2), ctx, "bin_images");
+    }
+    check(emc_mem_free(ctx, d_raw), ctx, "free");
+    check(emc_mem_free(ctx, d_raw_mask), ctx, "free");
+  } else {
+    check(emc_copy_real_to_device(ctx, images.data(), d_images, N * n2), ctx, "copy");
+  }
+  if (cfg.model_input == 0 || cfg.model_input == 2)
+    check(emc_copy_real_to_device(ctx, model.data(), d_model, (int)n3), ctx, "copy");
   check(emc_copy_real_to_device(ctx, x.data(), d_x, n2), ctx, "copy");
   check(emc_copy_real_to_device(ctx, y.data(), d_y, n2), ctx, "copy");
   check(emc_copy_real_to_device(ctx, z.data(), d_z, n2), ctx, "copy");
   check(emc_copy_real_to_device(ctx, quats.data(), d_rot, 4 * R), ctx, "copy");
   check(emc_copy_real_to_device(ctx, rotw.data(), d_w, R), ctx, "copy");
   check(emc_copy_int_to_device(ctx, mask.data(), d_mask, n2), ctx, "copy");
+  // normalize_images (main.cpp:96-98).  The fused plan folds the per-pattern
+  // factor into the scaling itself (so the tensor cores keep integer counts);
+  // the drop-in path and the model initialisation take normalised patterns.
+  float* d_norm = d_images;
+  if (cfg.normalize_images) {
+    if (o.dropin) {
+      check(emc_normalize_images(ctx, d_images, d_mask, nullptr, n2, N), ctx, "normalize_images");
+    } else if (cfg.model_input == 1 || cfg.model_input == 3) {
+      check(emc_allocate_real(ctx, &d_norm, (size_t)N * n2), ctx, "alloc");
+      check(emc_copy_real_d2d(ctx, d_norm, d_images, 0, N * n2), ctx, "copy");
+      check(emc_normalize_images(ctx, d_norm, d_mask, nullptr, n2, N), ctx, "normalize_images");
+    }
+  }
+  if (cfg.model_input == 3) {  // radial average (emc_helper.cpp:458-502)
+    check(emc_model_init_radial(ctx, d_norm, N, side, d_model), ctx, "model_init_radial");
+  } else if (cfg.model_input == 1) {  // random orientations (emc_helper.cpp:503-518)
+    std::vector<float> q(4 * (size_t)N);
+    if (emc_random_rotations(0, N, q.data()) != 0) die("random rotations failed");
+    float* d_q = nullptr;
+    check(emc_allocate_real(ctx, &d_q, 4 * (size_t)N), ctx, "alloc");
+    check(emc_copy_real_to_device(ctx, q.data(), d_q, 4 * N), ctx, "copy");
+    check(emc_model_init_orientations(ctx, d_norm, d_mask, N, side, d_q, d_x, d_y, d_z, d_model,
+                                      d_weight), ctx, "model_init_orientations");
+    check(emc_mem_free(ctx, d_q), ctx, "free");
+  }
+  if (d_norm != d_images) check(emc_mem_free(ctx, d_norm), ctx, "free");
+  if (d_masks) check(emc_mask_images(ctx, d_images, d_masks, n2, N), ctx, "mask_images");
   check(emc_normalize_model(ctx, side, d_model, nullptr), ctx, "normalize");  // main.cpp:180
 
   emc_plan* plan = nullptr;
@@ -207,18 +276,17 @@ int main(int argc, char** argv) {
     d.normalize_images = cfg.normalize_images;
     d.blur_sigma = (float)cfg.model_blur;
     check(emc_plan_create(ctx, &d, &plan), ctx, "plan_create");
-    check(emc_plan_bind(plan, d_images, d_mask, d_x, d_y, d_z, d_rot, d_w), ctx, "plan_bind");
-  } else {
-    if (cfg.normalize_images) {  // emc_helper.cpp:389-418 on the host, float sums
-      for (int i = 0; i < N; ++i) {
-        float s = 0.0f;
-        for (int p = 0; p < n2; ++p)
-          if (mask[p] == 1) s += images[(size_t)i * n2 + p];
-        const float c = (float)n2 / s;
-        for (int p = 0; p < n2; ++p) images[(size_t)i * n2 + p] *= c;
-      }
-      check(emc_copy_real_to_device(ctx, images.data(), d_images, N * n2), ctx, "copy");
+    int rc = emc_plan_bind(plan, d_images, d_mask, d_x, d_y, d_z, d_rot, d_w);
+    if (rc == EMC_ERR_UNSUPPORTED && d.precision == EMC_PREC_MIXED) {
+      // e.g. -1 at per-pattern masked pixels: not an FP16 count
+      std::fprintf(stderr, "emc: %s; using the FP32 path\n", emc_last_error(ctx));
+      emc_plan_destroy(plan);
+      d.precision = EMC_PREC_FP32;
+      check(emc_plan_create(ctx, &d, &plan), ctx, "plan_create");
+      rc = emc_plan_bind(plan, d_images, d_mask, d_x, d_y, d_z, d_rot, d_w);
     }
+    check(rc, ctx, "plan_bind");
+  } else {
     check(emc_allocate_real(ctx, &d_resp, (size_t)R * N), ctx, "alloc");
     check(emc_allocate_real(ctx, &d_scal, (size_t)R * N), ctx, "alloc");
     check(emc_allocate_real(ctx, &d_slices, (size_t)chunk * n2), ctx, "alloc");

@@ -322,3 +322,31 @@ extern "C" int emc_generate_rotations(int n, float* quats, float* weights, int c
   }
   return n_keep;
 }
+
+// quaternion_random (rotations.c:30-41) with this library's own generator in
+// place of GSL's: u = top 53 bits of splitmix64(seed, k) / 2^53, stored as
+// `real` (float) like gsl_rng_uniform's result, then
+// q = (sqrt(1-u1) sin(2 pi u2), sqrt(1-u1) cos(2 pi u2), sqrt(u1) sin(2 pi u3),
+// sqrt(u1) cos(2 pi u3)) in double, stored as float.
+static uint64_t splitmix64(uint64_t& s) {
+  uint64_t z = (s += 0x9E3779B97F4A7C15ULL);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+  return z ^ (z >> 31);
+}
+
+extern "C" int emc_random_rotations(unsigned long long seed, int n, float* quats) {
+  if (n < 0 || (n > 0 && !quats)) return -1;
+  uint64_t s = seed;
+  const double two_pi = 2.0 * 3.14159265358979323846;
+  for (int i = 0; i < n; ++i) {
+    float u[3];
+    for (float& v : u) v = (float)((double)(splitmix64(s) >> 11) * (1.0 / 9007199254740992.0));
+    const double a = std::sqrt((double)(1.0f - u[0])), b = std::sqrt((double)u[0]);
+    quats[4 * i + 0] = (float)(a * std::sin(two_pi * u[1]));
+    quats[4 * i + 1] = (float)(a * std::cos(two_pi * u[1]));
+    quats[4 * i + 2] = (float)(b * std::sin(two_pi * u[2]));
+    quats[4 * i + 3] = (float)(b * std::cos(two_pi * u[2]));
+  }
+  return 0;
+}

@@ -199,25 +199,35 @@ def make_problem(cfg: Config, device: str | None = None, coords=None, rotations=
     return Problem(cfg, true.reshape(-1), init, images, mask, x, y, z, quats, weights, tq, scales)
 
 
-def write_problem(prob: Problem, directory, iterations=1, extra=""):
+def write_problem(prob: Problem, directory, iterations=1, extra="", model_input=2,
+                  normalize_images=False, raw=None, read_stride=1):
     """Writes the `emc` driver's inputs: images.bin (float32 [N][s*s]),
     mask.bin (int32 [s*s]), model.bin (float32 [s^3], read with model_input 2)
-    and an emc.conf that points at them.  Returns the config path."""
+    and an emc.conf that points at them.  With raw = (frames [N][D][D],
+    masks [N][D][D]) it writes raw.bin / raw_mask.bin instead of images.bin,
+    for binning by read_stride.  Returns the config path."""
     import os
     d = os.path.abspath(str(directory))
     os.makedirs(d, exist_ok=True)
     c = prob.cfg
-    np.ascontiguousarray(prob.images, np.float32).tofile(os.path.join(d, "images.bin"))
+    detector = c.side
+    if raw is None:
+        np.ascontiguousarray(prob.images, np.float32).tofile(os.path.join(d, "images.bin"))
+    else:
+        frames, fmasks = raw
+        detector = frames.shape[-1]
+        np.ascontiguousarray(frames, np.float32).tofile(os.path.join(d, "raw.bin"))
+        np.ascontiguousarray(fmasks, np.int32).tofile(os.path.join(d, "raw_mask.bin"))
     np.ascontiguousarray(prob.mask, np.int32).tofile(os.path.join(d, "mask.bin"))
     np.ascontiguousarray(prob.init_model, np.float32).tofile(os.path.join(d, "model.bin"))
     conf = os.path.join(d, "emc.conf")
     with open(conf, "w") as f:
         f.write(f"""# synthetic problem {c.name}
 model_side = {c.side};
-read_stride = 1;
+read_stride = {read_stride};
 wavelength = {WAVELENGTH!r};
 pixel_size = {PIXEL_SIZE!r};
-detector_size = {c.side};
+detector_size = {detector};
 detector_distance = {DISTANCE!r};
 rotations_n = {c.rot_n};
 sigma_start = {SIGMA_START};
@@ -229,9 +239,9 @@ N_images = {c.n_images};
 max_iterations = {iterations};
 image_prefix = "{d}/";
 mask_file = "{d}/mask.bin";
-normalize_images = false;
+normalize_images = {"true" if normalize_images else "false"};
 known_intensity = false;
-model_input = 2;
+model_input = {model_input};
 model_file = "{d}/model.bin";
 isOutput = 1;
 output_loop = 0;

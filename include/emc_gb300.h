@@ -92,6 +92,10 @@ int emc_calculate_coordinates(int side, float pixel_size, float detector_distanc
 /* main.cpp:251: sigma_t = sf + (ss - sf) * exp(-t / half_life * ln 2). */
 float emc_sigma_schedule(int iteration, double sigma_start, double sigma_final, int half_life);
 
+/* rotations.c:30-41 quaternion_random, n times, with this library's seeded
+ * generator (splitmix64) in place of GSL's gsl_rng_taus: 4*n floats (host). */
+int emc_random_rotations(unsigned long long seed, int n, float* quats);
+
 /* ---- configuration (emc.conf) ------------------------------------------ */
 /* The keys of Configuration (configs.h:11-89) read by configs.cpp:40-90. */
 #define EMC_CONFIG_PATH_MAX 512
@@ -234,6 +238,39 @@ int emc_copy_int_to_device(emc_ctx* ctx, const int* h_src, int* d_dst, int n);
 int emc_allocate_real(emc_ctx* ctx, float** d_out, size_t n);
 int emc_allocate_int(emc_ctx* ctx, int** d_out, size_t n);
 int emc_mem_free(emc_ctx* ctx, void* d_ptr);
+
+/* ---- preprocessing and model initialisation (main.cpp:92-108) ---------- */
+/* read_images binning (emc_helper.cpp:226-243): raw patterns
+ * [n_images][raw_h][raw_w] and their masks (int, x fastest) -> images
+ * [n_images][side*side] = (sum of |raw|) / (sum of the raw mask) over the
+ * stride x stride block of each output pixel, and per-pattern masks
+ * [n_images][side*side] = 1 where that mask sum is > 1.  The block of output
+ * pixel o starts at (int)(stride ((o - side/2) + 0.5) + raw/2 - 0.5) per axis;
+ * raw pixels outside the frame count as 0. */
+int emc_bin_images(emc_ctx* ctx, const float* d_raw, const int* d_raw_mask, int raw_w, int raw_h,
+                   int n_images, int side, int stride, float* d_images, int* d_masks);
+/* normalize_images_central_part (emc_helper.cpp:389-418; its central mask is
+ * all ones, so the factor is N_2d / sum over d_mask == 1) or, with d_masks,
+ * normalize_images_individual_mask (:421-438): images *= N_2d / (float sum of
+ * the pattern's pixels whose mask is 1), summed in pixel order. */
+int emc_normalize_images(emc_ctx* ctx, float* d_images, const int* d_mask, const int* d_masks,
+                         int N_2d, int n_images);
+/* mask_model (emc_helper.cpp:567-575): images = -1 where d_masks == 0. */
+int emc_mask_images(emc_ctx* ctx, float* d_images, const int* d_masks, int N_2d, int n_images);
+/* model_init with model_input 3 (emc_helper.cpp:458-502): the radial average
+ * of all patterns, interpolated linearly in radius; -1 outside radius side/2.
+ * Ring sums are FP64 (the reference sums in float). */
+int emc_model_init_radial(emc_ctx* ctx, const float* d_images, int n_images, int side,
+                          float* d_model);
+/* model_init with model_input 1 (emc_helper.cpp:503-518): pattern i inserted
+ * once with weight 1 at quaternion d_rot[i] (e.g. emc_random_rotations) by
+ * the reference's host insert_slice arithmetic (emc_helper.cpp:81-135:
+ * round(side/2 + 0.5 + c)); then model = model / weight where weight > 0,
+ * else 0. */
+int emc_model_init_orientations(emc_ctx* ctx, const float* d_images, const int* d_mask,
+                                int n_images, int side, const float* d_rot, const float* d_x,
+                                const float* d_y, const float* d_z, float* d_model,
+                                float* d_weight);
 
 /* ---- fused iteration (the fast path) ----------------------------------- */
 typedef struct {

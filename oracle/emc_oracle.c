@@ -26,6 +26,9 @@
  *   insert          emc_atomic.cu:33-85, 183-200
  *   divide          emc_cuda.cu:758-786
  *   model average   emc_cuda.cu:639-671, 788-798
+ *   preprocessing   emc_helper.cpp:226-243 (binning), 389-438 (normalise),
+ *                   567-575 (per-pattern masks), 458-518 (model init 3 and 1),
+ *                   81-135 (host insert_slice)
  */
 #include <math.h>
 #include <stdint.h>
@@ -368,4 +371,152 @@ void oracle_trilinear_stencil(const float* rot, int R, const float* xc, const fl
       }
     }
   }
+}
+
+/* ---- preprocessing and model initialisation (host code of the reference) -- */
+
+/* read_images binning, emc_helper.cpp:226-243: output (x, y) sums |raw| and
+ * the raw mask over a stride x stride block starting at
+ * (int)(stride * ((real)(o - side/2) + 0.5) + raw/2 - 0.5) per axis (double
+ * arithmetic, xb outer, yb inner); value = float sum / (real)mask sum, mask =
+ * mask sum > 1.  Raw pixels outside the frame count as 0 (the reference
+ * reads them unchecked).  Layouts: raw [n][raw_h][raw_w], out [n][side][side],
+ * x fastest. */
+void oracle_bin_images(const float* raw, const int* raw_mask, int raw_w, int raw_h, int n,
+                       int side, int stride, float* images, int* masks) {
+  for (int i = 0; i < n; ++i)
+    for (int y = 0; y < side; ++y)
+      for (int x = 0; x < side; ++x) {
+        const int sx0 = (int)(stride * ((double)(float)(x - side / 2) + 0.5) + raw_w / 2 - 0.5);
+        const int sy0 = (int)(stride * ((double)(float)(y - side / 2) + 0.5) + raw_h / 2 - 0.5);
+        float psum = 0.0f;
+        int msum = 0;
+        for (int xb = 0; xb < stride; ++xb)
+          for (int yb = 0; yb < stride; ++yb) {
+            const int sx = sx0 + xb, sy = sy0 + yb;
+            if (sx < 0 || sx >= raw_w || sy < 0 || sy >= raw_h) continue;
+            const size_t e = ((size_t)i * raw_h + sy) * raw_w + sx;
+            psum += fabsf(raw[e]);
+            msum += raw_mask[e];
+          }
+        const size_t o = ((size_t)i * side + y) * side + x;
+        images[o] = psum / (float)msum;
+        masks[o] = msum > 1 ? 1 : 0;
+      }
+}
+
+/* normalize_images_central_part (emc_helper.cpp:389-418, whose central mask
+ * is 1 everywhere) and normalize_images_individual_mask (:421-438, masks !=
+ * NULL): factor (real)N_2d / (sequential float sum where mask == 1), images
+ * *= factor.  Returns the factors in factor[n]. */
+void oracle_normalize_images(float* images, const int* mask, const int* masks, int n2, int n,
+                             float* factor) {
+  for (int i = 0; i < n; ++i) {
+    const int* m = masks ? masks + (size_t)i * n2 : mask;
+    float sum = 0.0f;
+    for (int p = 0; p < n2; ++p)
+      if (m[p] == 1) sum += images[(size_t)i * n2 + p];
+    sum = (float)n2 / sum;
+    factor[i] = sum;
+    for (int p = 0; p < n2; ++p) images[(size_t)i * n2 + p] *= sum;
+  }
+}
+
+/* mask_model, emc_helper.cpp:567-575. */
+void oracle_mask_images(float* images, const int* masks, long n) {
+  for (long e = 0; e < n; ++e)
+    if (masks[e] == 0) images[e] = -1.0f;
+}
+
+/* model_init, model_input 3, emc_helper.cpp:458-502.  radavg[r] accumulates
+ * pattern values in float over i, x, y (sequential, as the reference) when
+ * float_sums, else in double; then radavg /= (real)count.  radavg has side/2
+ * + 1 entries, the last 0 (the reference reads one past its array).  The
+ * model value is computed in double and stored as float; -1 outside. */
+void oracle_model_init_radial(const float* images, int n, int side, int float_sums,
+                              float* radavg_out, float* model) {
+  const int nr = side / 2;
+  float* radavg = (float*)calloc((size_t)nr + 1, sizeof(float));
+  double* dsum = (double*)calloc((size_t)nr + 1, sizeof(double));
+  int* cnt = (int*)calloc((size_t)nr + 1, sizeof(int));
+  const double h = (double)side / 2.0;
+  for (int i = 0; i < n; ++i)
+    for (int x = 0; x < side; ++x)
+      for (int y = 0; y < side; ++y) {
+        const double dx = (double)(float)x - h + 0.5, dy = (double)(float)y - h + 0.5;
+        const int r = (int)sqrt(dx * dx + dy * dy);
+        if (r < h) {
+          const float v = images[((size_t)i * side + y) * side + x];
+          if (float_sums)
+            radavg[r] += v;
+          else
+            dsum[r] += (double)v;
+          cnt[r] += 1;
+        }
+      }
+  for (int r = 0; r < nr; ++r) {
+    if (!float_sums) radavg[r] = (float)dsum[r];
+    radavg[r] = cnt[r] > 0 ? radavg[r] / (float)cnt[r] : 0.0f;
+  }
+  radavg[nr] = 0.0f;
+  for (int x = 0; x < side; ++x)
+    for (int y = 0; y < side; ++y)
+      for (int z = 0; z < side; ++z) {
+        const double dx = (double)(float)x - h + 0.5, dy = (double)(float)y - h + 0.5,
+                     dz = (double)(float)z - h + 0.5;
+        const double rad = sqrt(dx * dx + dy * dy + dz * dz);
+        const int r = (int)rad;
+        const size_t v = ((size_t)z * side + y) * side + x;
+        if (r < h)
+          model[v] = (float)(radavg[r] * (1.0 - (rad - (double)r)) +
+                             radavg[r + 1] * (rad - (double)r));
+        else
+          model[v] = -1.0f;
+      }
+  if (radavg_out) memcpy(radavg_out, radavg, sizeof(float) * ((size_t)nr + 1));
+  free(radavg);
+  free(dsum);
+  free(cnt);
+}
+
+/* Voxel of pixel p of the common mask for quaternion q under the host
+ * insert_slice (emc_helper.cpp:81-135): float diagonal terms, double
+ * off-diagonal terms (2.0 * ...), coordinate sums in double stored to float,
+ * round(side/2.0 + 0.5 + c), bounds [0, side).  Returns -1 outside. */
+static long host_insert_voxel(const float* q, int side, float x, float y, float z) {
+  const float q0 = q[0], q1 = q[1], q2 = q[2], q3 = q[3];
+  const float nx = (q0 * q0 + q1 * q1 - q2 * q2 - q3 * q3) * x +
+                   (2.0 * q1 * q2 - 2.0 * q0 * q3) * y + (2.0 * q1 * q3 + 2.0 * q0 * q2) * z;
+  const float ny = (2.0 * q1 * q2 + 2.0 * q0 * q3) * x +
+                   (q0 * q0 - q1 * q1 + q2 * q2 - q3 * q3) * y +
+                   (2.0 * q2 * q3 - 2.0 * q0 * q1) * z;
+  const float nz = (2.0 * q1 * q3 - 2.0 * q0 * q2) * x + (2.0 * q2 * q3 + 2.0 * q0 * q1) * y +
+                   (q0 * q0 - q1 * q1 - q2 * q2 + q3 * q3) * z;
+  const int rx = (int)round((float)side / 2.0 + 0.5 + nx);
+  const int ry = (int)round((float)side / 2.0 + 0.5 + ny);
+  const int rz = (int)round((float)side / 2.0 + 0.5 + nz);
+  if (rx < 0 || rx >= side || ry < 0 || ry >= side || rz < 0 || rz >= side) return -1;
+  return ((long)rz * side + ry) * side + rx;
+}
+
+/* model_init, model_input 1, emc_helper.cpp:503-518: every pattern inserted
+ * once, weight 1, at quats[i] (in pattern order, pixels x outer, y inner as
+ * insert_slice), then model /= weight where weight > 0, else 0. */
+void oracle_model_init_orientations(const float* images, const int* mask, int n, int side,
+                                    const float* quats, const float* xc, const float* yc,
+                                    const float* zc, float* model, float* weight) {
+  const long n3 = (long)side * side * side;
+  memset(model, 0, sizeof(float) * n3);
+  memset(weight, 0, sizeof(float) * n3);
+  for (int i = 0; i < n; ++i)
+    for (int x = 0; x < side; ++x)
+      for (int y = 0; y < side; ++y) {
+        const int p = y * side + x;
+        if (mask[p] != 1) continue;
+        const long v = host_insert_voxel(quats + 4 * (size_t)i, side, xc[p], yc[p], zc[p]);
+        if (v < 0) continue;
+        model[v] = model[v] + 1.0f * images[(size_t)i * side * side + p];
+        weight[v] = weight[v] + 1.0f;
+      }
+  for (long v = 0; v < n3; ++v) model[v] = weight[v] > 0.0f ? model[v] / weight[v] : 0.0f;
 }

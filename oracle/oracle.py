@@ -55,6 +55,12 @@ def lib():
         i64p = np.ctypeslib.ndpointer(np.int64, flags="C_CONTIGUOUS")
         l.oracle_nearest_voxels.argtypes = [f32p, I, f32p, f32p, f32p, I, I, I, i64p]
         l.oracle_trilinear_stencil.argtypes = [f32p, I, f32p, f32p, f32p, I, I, i64p, f32p]
+        l.oracle_bin_images.argtypes = [f32p, i32p, I, I, I, I, I, f32p, i32p]
+        l.oracle_normalize_images.argtypes = [f32p, i32p, C.c_void_p, I, I, f32p]
+        l.oracle_mask_images.argtypes = [f32p, i32p, L]
+        l.oracle_model_init_radial.argtypes = [f32p, I, I, I, f32p, f32p]
+        l.oracle_model_init_orientations.argtypes = [f32p, i32p, I, I, f32p, f32p, f32p, f32p,
+                                                     f32p, f32p]
         _lib = l
     return _lib
 
@@ -339,3 +345,52 @@ def blur_fft_fp64(model, side, sigma):
     Mul = m1[:, None, None] * m1[None, :, None] * m1[None, None, :]
     out = np.fft.ifftn(np.fft.fftn(v) * Mul).real
     return np.where(keep, out, -1.0).reshape(-1)
+
+
+# ------------------------------------------------------ preprocessing ----
+def bin_images(raw, raw_mask, side, stride):
+    """read_images binning (emc_helper.cpp:226-243): raw [n, h, w] -> (images [n, side*side],
+    masks [n, side*side])."""
+    raw, raw_mask = _f(raw), _i(raw_mask)
+    n, h, w = raw.shape
+    images = np.zeros((n, side * side), np.float32)
+    masks = np.zeros((n, side * side), np.int32)
+    lib().oracle_bin_images(raw, raw_mask, w, h, n, side, stride, images, masks)
+    return images, masks
+
+
+def normalize_images(images, mask, masks=None):
+    """normalize_images_central_part / _individual_mask (emc_helper.cpp:389-438)."""
+    out = _f(images).copy()
+    n, n2 = out.shape
+    fac = np.zeros(n, np.float32)
+    mk = None if masks is None else _i(masks)
+    lib().oracle_normalize_images(out, _i(mask), None if mk is None else mk.ctypes.data, n2, n,
+                                  fac)
+    return out, fac
+
+
+def mask_images(images, masks):
+    out = _f(images).copy()
+    lib().oracle_mask_images(out, _i(masks), out.size)
+    return out
+
+
+def model_init_radial(images, side, float_sums=True):
+    """model_init, model_input 3 (emc_helper.cpp:458-502); float_sums=True is the
+    reference's sequential float ring sums, False FP64 ring sums."""
+    images = _f(images)
+    radavg = np.zeros(side // 2 + 1, np.float32)
+    model = np.zeros(side ** 3, np.float32)
+    lib().oracle_model_init_radial(images, images.shape[0], side, int(float_sums), radavg, model)
+    return model, radavg
+
+
+def model_init_orientations(images, mask, side, quats, x, y, z):
+    """model_init, model_input 1 (emc_helper.cpp:503-518) at the given quaternions."""
+    images = _f(images)
+    model = np.zeros(side ** 3, np.float32)
+    weight = np.zeros(side ** 3, np.float32)
+    lib().oracle_model_init_orientations(images, _i(mask), images.shape[0], side, _f(quats),
+                                         _f(x), _f(y), _f(z), model, weight)
+    return model, weight

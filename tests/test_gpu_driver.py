@@ -76,3 +76,30 @@ def test_dropin_driver_matches_reference_oracle(prob, tmp_path):
     got_m = np.fromfile(tmp_path / "out" / "output" / "model_0000.bin", np.float32)
     ok = (want["weight"] > 0) & (want["model"] > 0)
     np.testing.assert_allclose(got_m, np.where(ok, want["model"], 0), rtol=2e-5, atol=1e-6)
+
+
+def test_driver_bins_raw_frames(prob, tmp_path):
+    """Frames whose 2x2 blocks repeat each pattern value bin back to the
+    patterns exactly (sum 4k / mask sum 4), so the run equals the one from the
+    binned patterns bit for bit."""
+    frames = np.repeat(np.repeat(prob.images.reshape(-1, prob.cfg.side, prob.cfg.side), 2, 1), 2, 2)
+    fmasks = np.ones(frames.shape, np.int32)
+    a = run_driver(S.write_problem(prob, tmp_path / "a", iterations=1), tmp_path / "oa",
+                   "--deterministic")
+    b = run_driver(S.write_problem(prob, tmp_path / "b", iterations=1, raw=(frames, fmasks),
+                                   read_stride=2), tmp_path / "ob", "--deterministic")
+    assert a[0]["total_loglik"] == b[0]["total_loglik"]
+    for name in ("model_0000.bin", "weight_0000.bin"):
+        assert np.array_equal(np.fromfile(tmp_path / "oa" / "output" / name, np.float32),
+                              np.fromfile(tmp_path / "ob" / "output" / name, np.float32))
+
+
+@pytest.mark.parametrize("model_input", [1, 3])
+@pytest.mark.parametrize("dropin", [False, True])
+def test_driver_model_init_modes(prob, tmp_path, model_input, dropin):
+    conf = S.write_problem(prob, tmp_path / "in", iterations=1, model_input=model_input,
+                           normalize_images=True)
+    logs = run_driver(conf, tmp_path / "out", *(["--dropin"] if dropin else []))
+    assert len(logs) == 1 and np.isfinite(logs[0]["total_loglik"])
+    m = np.fromfile(tmp_path / "out" / "output" / "model_0000.bin", np.float32)
+    assert np.all(np.isfinite(m)) and m.max() > 0

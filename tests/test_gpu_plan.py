@@ -242,3 +242,23 @@ def test_properties_at_small_config(ctx, cuda):
     inserted = (vox >= 0).sum(1)
     assert abs(a["weight"].sum() - (T_r * inserted).sum()) <= 1e-4 * a["weight"].sum()
     assert abs(a["stats"].captured_mass - 1.0) < 1e-5
+
+
+@pytest.fixture(scope="module")
+def lowcount():
+    # the low-count stress configuration's character at a size the FP64 oracle
+    # finishes quickly: 80 photons per pattern, scales U(0.2, 2.0), half of the
+    # detector masked by seeded panel gaps plus the beamstop
+    cfg = S.Config("lowcount-tiny", 32, 120, 1.2, 7.0, 400, 80.0, (0.2, 2.0), 2, 2, 1,
+                   masked_fraction=0.5)
+    return S.make_problem(cfg)
+
+
+@pytest.mark.parametrize("precision", [E.PREC_FP32, E.PREC_MIXED], ids=["fp32", "mixed"])
+def test_lowcount_matches_oracle_and_reruns_bit_identical(ctx, cuda, lowcount, precision):
+    assert lowcount.mask.sum() < 0.55 * (np.pi * 16 ** 2)
+    check_against_oracle(ctx, cuda, lowcount, dict(interp=E.INTERP_NEAREST), False, precision)
+    a = run_plan(ctx, lowcount, cuda, precision=precision, insert_mode=E.INSERT_DETERMINISTIC)
+    b = run_plan(ctx, lowcount, cuda, precision=precision, insert_mode=E.INSERT_DETERMINISTIC)
+    assert np.array_equal(a["model"], b["model"]) and np.array_equal(a["weight"], b["weight"])
+    assert np.array_equal(a["respons"], b["respons"])

@@ -25,7 +25,7 @@ from ._lib import (DIFF_ABSOLUTE, DIFF_POISSON, DIFF_RELATIVE, DIFF_TRUE_POISSON
                    PREC_FP32, PREC_MIXED, EmcError, IterStats, PlanDesc)
 
 __all__ = [
-    "Context", "Plan", "EmcError", "generate_rotations", "rotation_count",
+    "Context", "Plan", "Batch", "EmcError", "generate_rotations", "rotation_count",
     "calculate_coordinates", "sigma_schedule", "library",
 ]
 
@@ -367,6 +367,43 @@ class Plan:
     def close(self):
         if getattr(self, "_h", None):
             self._lib.emc_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Batch:
+    """Independent reconstructions run together: one graph launch per
+    iteration covers every plan (emc_batch_* in the C ABI)."""
+
+    def __init__(self, plans, models, weights):
+        n = len(plans)
+        self.plans = list(plans)
+        self._keep = (list(models), list(weights))
+        self._lib = plans[0]._lib
+        hp = (C.c_void_p * n)(*[p._h.value for p in plans])
+        hm = (C.c_void_p * n)(*[_ptr(m) for m in models])
+        hw = (C.c_void_p * n)(*[_ptr(w) for w in weights])
+        h = C.c_void_p()
+        plans[0].ctx._check(self._lib.emc_batch_create(hp, hm, hw, n, C.byref(h)), "batch_create")
+        self._h = h
+
+    def run(self, sigmas):
+        arr = (C.c_float * len(self.plans))(*[float(s) for s in sigmas])
+        self.plans[0].ctx._check(self._lib.emc_batch_run(self._h, arr), "batch_run")
+
+    def wait(self):
+        st = (IterStats * len(self.plans))()
+        self.plans[0].ctx._check(self._lib.emc_batch_wait(self._h, st), "batch_wait")
+        return list(st)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.emc_batch_destroy(self._h)
             self._h = None
 
     def __del__(self):

@@ -120,6 +120,10 @@ SIGNATURES: dict[str, tuple] = {
     "emc_plan_wait": (I, [P, C.POINTER(IterStats)]),
     "emc_plan_capture": (I, [P, P, P]),
     "emc_plan_replay": (I, [P, F]),
+    "emc_batch_create": (I, [P, P, P, I, C.POINTER(P)]),
+    "emc_batch_run": (I, [P, P]),
+    "emc_batch_wait": (I, [P, P]),
+    "emc_batch_destroy": (I, [P]),
     "emc_plan_results": (I, [P, C.POINTER(P), C.POINTER(P), C.POINTER(P)]),
     "emc_plan_set_profiling": (I, [P, I]),
     "emc_plan_set_option": (I, [P, I, I]),

@@ -1309,6 +1309,82 @@ extern "C" int emc_plan_replay(emc_plan* p, float sigma) {
   return EMC_OK;
 }
 
+// ---------------------------------------------------------------- batch --
+// Several independent reconstructions in one graph launch: each plan's
+// captured iteration becomes a child graph of one parent graph with no edges
+// between them, so the GPU runs them concurrently.
+struct emc_batch {
+  std::vector<emc_plan*> plans;
+  emc_ctx* ctx = nullptr;  // stream of the launches (the first plan's context)
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+};
+
+extern "C" int emc_batch_create(emc_plan** plans, float** d_models, float** d_weights, int n,
+                                emc_batch** out) {
+  if (!plans || !d_models || !d_weights || n <= 0 || !out || !plans[0]) return EMC_ERR_INVALID;
+  emc_ctx* ctx = plans[0]->ctx;
+  for (int k = 0; k < n; ++k) {
+    EMC_REQUIRE(ctx, plans[k] && d_models[k] && d_weights[k], "batch_create: null entry %d", k);
+    EMC_REQUIRE(ctx, plans[k]->ctx->device == ctx->device, "batch_create: plans on two devices");
+    const int rc = emc_plan_capture(plans[k], d_models[k], d_weights[k]);
+    if (rc) return fail(ctx, rc, "batch_create: plan %d: %s", k, emc_last_error(plans[k]->ctx));
+  }
+  emc_batch* b = new emc_batch();
+  b->plans.assign(plans, plans + n);
+  b->ctx = ctx;
+  cudaError_t e = cudaGraphCreate(&b->graph, 0);
+  for (int k = 0; k < n && e == cudaSuccess; ++k) {
+    cudaGraphNode_t node;
+    e = cudaGraphAddChildGraphNode(&node, b->graph, nullptr, 0, plans[k]->graph);
+  }
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&b->exec, b->graph, 0);
+  if (e != cudaSuccess) {
+    emc_batch_destroy(b);
+    return cuda_fail(ctx, e, "batch_create");
+  }
+  *out = b;
+  return EMC_OK;
+}
+
+extern "C" int emc_batch_run(emc_batch* b, const float* sigmas) {
+  if (!b || !sigmas) return EMC_ERR_INVALID;
+  emc_ctx* ctx = b->ctx;
+  for (size_t k = 0; k < b->plans.size(); ++k) {
+    const float sg = sigmas[k];
+    EMC_REQUIRE(ctx, sg > 0.0f && std::isfinite(sg), "batch_run: bad sigma %zu", k);
+    // pageable source: staged before the call returns, ordered before the launch
+    EMC_CUDA(ctx, cudaMemcpyAsync(b->plans[k]->sigma_dev, &sg, sizeof(float),
+                                  cudaMemcpyHostToDevice, ctx->stream));
+  }
+  EMC_CUDA(ctx, cudaGraphLaunch(b->exec, ctx->stream));
+  return EMC_OK;
+}
+
+extern "C" int emc_batch_wait(emc_batch* b, emc_iter_stats* stats) {
+  if (!b) return EMC_ERR_INVALID;
+  emc_ctx* ctx = b->ctx;
+  EMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  int first = EMC_OK;
+  for (size_t k = 0; k < b->plans.size(); ++k) {
+    emc_plan* p = b->plans[k];
+    const int rc = emc_plan_wait(p, stats ? stats + k : nullptr);
+    if (rc && !first) first = fail(ctx, rc, "batch: plan %zu: %s", k, emc_last_error(p->ctx));
+    // the status resets of emc_plan_wait run on the plan's own stream
+    cudaStreamSynchronize(p->ctx->stream);
+  }
+  return first;
+}
+
+extern "C" int emc_batch_destroy(emc_batch* b) {
+  if (!b) return EMC_OK;
+  if (b->ctx) cudaStreamSynchronize(b->ctx->stream);
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  if (b->graph) cudaGraphDestroy(b->graph);
+  delete b;
+  return EMC_OK;
+}
+
 extern "C" int emc_plan_set_option(emc_plan* p, int option, int value) {
   if (!p) return EMC_ERR_INVALID;
   emc_ctx* ctx = p->ctx;

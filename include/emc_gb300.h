@@ -330,6 +330,18 @@ int emc_plan_wait(emc_plan* plan, emc_iter_stats* stats);
  * emc_plan_wait for errors and stats.  Re-capture after emc_plan_bind. */
 int emc_plan_capture(emc_plan* plan, float* d_model, float* d_weight);
 int emc_plan_replay(emc_plan* plan, float sigma);
+/* Batched reconstructions (no counterpart in the reference): n bound plans,
+ * each with its own model/weight, captured (emc_plan_capture) and nested as
+ * independent child graphs of one graph; emc_batch_run launches one
+ * iteration of every plan (sigma per plan) in a single graph launch on the
+ * first plan's context stream, so the problems run concurrently;
+ * emc_batch_wait synchronises and fills stats[n] (may be NULL). */
+typedef struct emc_batch emc_batch;
+int emc_batch_create(emc_plan** plans, float** d_models, float** d_weights, int n,
+                     emc_batch** out);
+int emc_batch_run(emc_batch* batch, const float* sigmas);
+int emc_batch_wait(emc_batch* batch, emc_iter_stats* stats);
+int emc_batch_destroy(emc_batch* batch);
 /* Precision knobs of the tensor-core kernels.
  * EMC_OPT_ESTEP_GHLO: 1 (default) takes the likelihood's rotation-side
  * factors s/(s+c) and 1/(s+c) as FP16 hi + lo, 0 as FP16 hi only (4 instead

@@ -90,3 +90,33 @@ def test_replay_without_capture_is_an_error(ctx, cuda, prob):
     with pytest.raises(E.EmcError):
         plan.iterate_async(None, None, 0.3)
     plan.close()
+
+
+def test_batch_matches_each_plan(ctx, cuda):
+    """Three uneven problems in one graph launch: every model, weight and
+    log-likelihood equals that problem's own direct iteration."""
+    probs = [S.make_problem(S.tiny(side=s, n_images=n, rot_n=r, seed=k))
+             for k, (s, n, r) in enumerate([(16, 70, 1), (24, 200, 2), (32, 130, 2)])]
+    ctxs = [E.Context(0) for _ in probs]
+    kinds = [E.PREC_FP32, E.PREC_MIXED, E.PREC_MIXED]
+    direct, plans, models, weights = [], [], [], []
+    for c, p, prec in zip(ctxs, probs, kinds):
+        plan, m = bound_plan(c, p, cuda, precision=prec)
+        w = torch.empty_like(m)
+        st = plan.iterate(m, w, 0.35)
+        direct.append((m.cpu().numpy(), w.cpu().numpy(), st.total_loglik))
+        m2 = torch.as_tensor(np.ascontiguousarray(p.init_model), device=cuda)
+        plans.append(plan)
+        models.append(m2)
+        weights.append(torch.empty_like(m2))
+    batch = E.Batch(plans, models, weights)
+    batch.run([0.35] * 3)
+    stats = batch.wait()
+    for (dm, dw, ll), m, w, st in zip(direct, models, weights, stats):
+        assert np.array_equal(m.cpu().numpy(), dm)
+        assert np.array_equal(w.cpu().numpy(), dw)
+        assert st.total_loglik == ll
+    batch.close()
+    for plan, c in zip(plans, ctxs):
+        plan.close()
+        c.close()

@@ -16,6 +16,7 @@ context's last error text, where the reference printed and continued.
 from __future__ import annotations
 
 import ctypes as C
+import weakref
 
 import numpy as np
 
@@ -121,6 +122,7 @@ class Context:
             raise EmcError(f"emc_ctx_create(device={device}) failed: {_lib.ERRORS.get(rc, rc)}")
         self._h = h
         self.device = device
+        self._children = weakref.WeakSet()  # plans and batches, closed before the context
 
     # -- plumbing ------------------------------------------------------------
     @property
@@ -134,6 +136,9 @@ class Context:
 
     def close(self):
         if getattr(self, "_h", None):
+            kids = list(getattr(self, "_children", ()))
+            for child in sorted(kids, key=lambda c: not isinstance(c, Batch)):  # batches first
+                child.close()
             self._lib.emc_ctx_destroy(self._h)
             self._h = None
 
@@ -300,6 +305,7 @@ class Plan:
         ctx._check(self._lib.emc_plan_create(ctx.handle, C.byref(d), C.byref(h)), "plan_create")
         self._h = h
         self._bound = None
+        ctx._children.add(self)
 
     @property
     def workspace_bytes(self) -> int:
@@ -318,6 +324,32 @@ class Plan:
         self.ctx._check(self._lib.emc_iterate(self._h, _ptr(model), _ptr(weight), float(sigma),
                                               C.byref(st) if stats else None), "iterate")
         return st if stats else None
+
+    def set_pruning(self, on: bool = True, min_mass: float = 0.999, dilate: float = 1.0,
+                    full_every: int = 0):
+        """Pruned iterations (tensor-core path): see emc_plan_set_pruning."""
+        self.ctx._check(self._lib.emc_plan_set_pruning(self._h, int(on), float(min_mass),
+                                                       float(dilate), int(full_every)),
+                        "plan_set_pruning")
+
+    def prune_info(self) -> dict:
+        info = _lib.PruneInfo()
+        self.ctx._check(self._lib.emc_plan_prune_info(self._h, C.byref(info)), "plan_prune_info")
+        return {k: getattr(info, k) for k, _ in info._fields_}
+
+    def pattern_order(self):
+        """Input pattern index of each position of the last iteration's results."""
+        out = np.zeros(self.desc.n_images, np.int32)
+        self.ctx._check(self._lib.emc_plan_pattern_order(self._h, out.ctypes.data),
+                        "plan_pattern_order")
+        return out
+
+    def rotation_order(self):
+        """Input rotation index of each row of the last iteration's results."""
+        out = np.zeros(self.desc.n_rot, np.int32)
+        self.ctx._check(self._lib.emc_plan_rotation_order(self._h, out.ctypes.data),
+                        "plan_rotation_order")
+        return out
 
     def iterate_async(self, model, weight, sigma):
         """Enqueue one iteration; errors and stats come from wait()."""
@@ -391,6 +423,8 @@ class Batch:
         h = C.c_void_p()
         plans[0].ctx._check(self._lib.emc_batch_create(hp, hm, hw, n, C.byref(h)), "batch_create")
         self._h = h
+        for p in plans:  # the batch goes before any of its plans' contexts
+            p.ctx._children.add(self)
 
     def run(self, sigmas):
         arr = (C.c_float * len(self.plans))(*[float(s) for s in sigmas])

@@ -49,6 +49,15 @@ class IterStats(C.Structure):
     ]
 
 
+class PruneInfo(C.Structure):
+    _fields_ = [
+        ("pruned", I), ("fallback", I), ("active_fraction", D), ("core_fraction", D),
+        ("margin_mass", D),
+        ("nn_angle", D), ("pruned_iterations", C.c_longlong),
+        ("fallback_iterations", C.c_longlong), ("full_iterations", C.c_longlong),
+    ]
+
+
 PATH_MAX = 512
 
 
@@ -120,6 +129,10 @@ SIGNATURES: dict[str, tuple] = {
     "emc_plan_wait": (I, [P, C.POINTER(IterStats)]),
     "emc_plan_capture": (I, [P, P, P]),
     "emc_plan_replay": (I, [P, F]),
+    "emc_plan_set_pruning": (I, [P, I, F, F, I]),
+    "emc_plan_prune_info": (I, [P, C.POINTER(PruneInfo)]),
+    "emc_plan_pattern_order": (I, [P, P]),
+    "emc_plan_rotation_order": (I, [P, P]),
     "emc_batch_create": (I, [P, P, P, I, C.POINTER(P)]),
     "emc_batch_run": (I, [P, P]),
     "emc_batch_wait": (I, [P, P]),

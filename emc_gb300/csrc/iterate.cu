@@ -63,13 +63,16 @@ __global__ void gather_coords_kernel(const int* __restrict__ pix, const float* _
 
 // Per-pattern factor of the reference's image normalisation
 // (emc_helper.cpp:389-418): c_i = N_2d / (float sum over mask == 1 pixels).
+// Pattern position i of the plan holds input pattern perm[i] (perm == nullptr:
+// the identity) in this and the other pattern-side kernels.
 __global__ void pattern_norm_kernel(const float* __restrict__ images, const int* __restrict__ mask,
-                                    int n2, int N, int normalize, float* __restrict__ cnorm) {
+                                    int n2, int N, int normalize, float* __restrict__ cnorm,
+                                    const int* __restrict__ perm) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= N) return;
   float c = 1.0f;
   if (normalize) {
-    const float* img = images + (size_t)i * n2;
+    const float* img = images + (size_t)(perm ? perm[i] : i) * n2;
     float s = 0.0f;
     for (int p = 0; p < n2; ++p)
       if (__ldg(mask + p) == 1) s = __fadd_rn(s, __ldg(img + p));
@@ -83,14 +86,15 @@ __global__ void pattern_norm_kernel(const float* __restrict__ images, const int*
 __global__ void pattern_ops_kernel(const float* __restrict__ images, const int* __restrict__ pix,
                                    const float* __restrict__ cnorm, int n2, int N, int Kp,
                                    float* __restrict__ Kraw, float* __restrict__ Kt,
-                                   float* __restrict__ K2, int* __restrict__ flags) {
+                                   float* __restrict__ K2, int* __restrict__ flags,
+                                   const int* __restrict__ perm) {
   const int i = blockIdx.y;
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= Kp) return;
   const int p = pix[q];
   float k = 0.0f;
   if (p >= 0) {
-    const float v = __ldg(images + (size_t)i * n2 + p);
+    const float v = __ldg(images + (size_t)(perm ? perm[i] : i) * n2 + p);
     if (!isfinite(v)) atomicOr(flags, 1);
     if (!(v >= 0.0f && v <= 2048.0f && v == rintf(v))) atomicOr(flags, 2);
     k = __fmul_rn(v, __ldg(cnorm + i));
@@ -550,6 +554,12 @@ __global__ void lse_combine_kernel(const float2* __restrict__ part, int n_rt, in
   lse2[n] = make_float2(hi, isfinite(l) ? (float)(l - (double)hi) : 0.0f);
 }
 
+__global__ void fill_part_kernel(float2* __restrict__ part, size_t n) {
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += stride)
+    part[e] = make_float2(-INFINITY, 0.0f);
+}
+
 // Deterministic FP64 sum of the finite entries of x[0..n) into out[0]
 // (one block; the order of additions is fixed).
 __global__ void finite_sum_kernel(const double* __restrict__ x, int n, double* __restrict__ out) {
@@ -584,18 +594,26 @@ __global__ void __launch_bounds__(kMprepThreads) mprep_kernel(
     const float* __restrict__ Ksum, const float* __restrict__ cnorm, int R, int N,
     float* __restrict__ Q, __half* __restrict__ Qh, __half* __restrict__ Ql,
     float* __restrict__ qscale, int ldq, float* __restrict__ T, double* __restrict__ row_mass,
-    double* __restrict__ row_bound, int stage) {
+    double* __restrict__ row_bound, int stage, const unsigned char* __restrict__ tstate,
+    int n_rt, double* __restrict__ row_margin) {
   extern __shared__ float qrow[];  // [N] when stage: the row's P c_i / phi
   const int r = blockIdx.x;
-  float t = 0.0f, b = 0.0f, qmax = 0.0f;
+  // pruned iteration: tstate[pattern tile][rotation tile] = 0 not evaluated
+  // (P = 0), 1 evaluated, 2 evaluated margin tile (its mass is summed)
+  const unsigned char* ts = tstate ? tstate + (r >> 7) : nullptr;
+  float t = 0.0f, b = 0.0f, qmax = 0.0f, mg = 0.0f;
   for (int i = threadIdx.x; i < N; i += blockDim.x) {
     const size_t e = (size_t)r * N + i;
-    const float2 li = lse2[i];
-    const float l = L[e];
-    float P = 0.0f;
-    if (isfinite(li.x) && l > -INFINITY) P = expf((l - li.x) - li.y);
+    const int st = ts ? ts[(size_t)(i >> 7) * n_rt] : 1;
+    float P = 0.0f, f = 0.0f;
+    if (st) {
+      const float2 li = lse2[i];
+      const float l = L[e];
+      if (isfinite(li.x) && l > -INFINITY) P = expf((l - li.x) - li.y);
+      f = PHI[e];
+      if (st == 2) mg += P;
+    }
     L[e] = P;
-    const float f = PHI[e];
     float q = f > 0.0f ? __fdiv_rn(P, f) : 0.0f;
     t += P;
     b = __fmaf_rn(q, __ldg(Ksum + i), b);
@@ -606,16 +624,18 @@ __global__ void __launch_bounds__(kMprepThreads) mprep_kernel(
   }
   if (Q)
     for (int i = N + threadIdx.x; i < ldq; i += blockDim.x) Q[(size_t)r * ldq + i] = 0.0f;
-  __shared__ double sh[2][kMprepThreads];
+  __shared__ double sh[3][kMprepThreads];
   __shared__ float smx[kMprepThreads];
   sh[0][threadIdx.x] = (double)t;
   sh[1][threadIdx.x] = (double)b;
+  sh[2][threadIdx.x] = (double)mg;
   smx[threadIdx.x] = qmax;
   __syncthreads();
   for (int o = blockDim.x / 2; o > 0; o >>= 1) {
     if (threadIdx.x < o) {
       sh[0][threadIdx.x] += sh[0][threadIdx.x + o];
       sh[1][threadIdx.x] += sh[1][threadIdx.x + o];
+      sh[2][threadIdx.x] += sh[2][threadIdx.x + o];
       smx[threadIdx.x] = fmaxf(smx[threadIdx.x], smx[threadIdx.x + o]);
     }
     __syncthreads();
@@ -624,6 +644,7 @@ __global__ void __launch_bounds__(kMprepThreads) mprep_kernel(
     T[r] = (float)sh[0][0];
     row_mass[r] = sh[0][0];
     row_bound[r] = sh[1][0];
+    if (row_margin) row_margin[r] = sh[2][0];
   }
   if (!Qh) return;
   const float mx = smx[0];
@@ -935,6 +956,7 @@ extern "C" int emc_plan_create(emc_ctx* ctx, const emc_plan_desc* desc, emc_plan
 extern "C" int emc_plan_destroy(emc_plan* p) {
   if (!p) return EMC_OK;
   if (p->ctx) cudaStreamSynchronize(p->ctx->stream);
+  prune_free(p);
   if (p->graph_exec) cudaGraphExecDestroy(p->graph_exec);
   if (p->graph) cudaGraphDestroy(p->graph);
   for (auto& e : p->ev)
@@ -946,6 +968,26 @@ extern "C" int emc_plan_destroy(emc_plan* p) {
 }
 
 extern "C" size_t emc_plan_workspace_bytes(const emc_plan* p) { return p ? p->bytes : 0; }
+
+// The pattern-side operands (per-pattern factor, compacted counts, their
+// sums, and the tensor-core forms once those exist) for the pattern order
+// perm (device [N]: position -> input pattern; nullptr: input order).
+int emc::pattern_side(emc_plan* p, const int* d_perm, bool with_tc) {
+  emc_ctx* ctx = p->ctx;
+  const int n2 = p->n2, N = p->d.n_images;
+  int rc;
+  pattern_norm_kernel<<<ceil_div(N, 128), 128, 0, ctx->stream>>>(
+      p->images, p->mask, n2, N, p->d.normalize_images, p->cnorm, d_perm);
+  if ((rc = after_launch(ctx, "pattern_norm_kernel"))) return rc;
+  // Kt / K2 exist only for the FP32 path (null: not written).
+  pattern_ops_kernel<<<dim3(ceil_div(p->Kp, 256), N), 256, 0, ctx->stream>>>(
+      p->images, p->pix, p->cnorm, n2, N, p->Kp, p->Kraw, p->Kt, p->K2, p->flags, d_perm);
+  if ((rc = after_launch(ctx, "pattern_ops_kernel"))) return rc;
+  row_sum_kernel<<<N, 256, 0, ctx->stream>>>(p->Kraw, p->Kp, p->Kp, p->Ksum);
+  if ((rc = after_launch(ctx, "row_sum_kernel"))) return rc;
+  if (with_tc && p->tc) return tc_pattern_side(p, d_perm);
+  return EMC_OK;
+}
 
 extern "C" int emc_plan_bind(emc_plan* p, const float* d_images, const int* d_mask,
                              const float* d_x, const float* d_y, const float* d_z,
@@ -1007,15 +1049,9 @@ extern "C" int emc_plan_bind(emc_plan* p, const float* d_images, const int* d_ma
   gather_coords_kernel<<<ceil_div(p->Kp, 256), 256, 0, ctx->stream>>>(p->pix, d_x, d_y, d_z, p->cx,
                                                                       p->cy, p->cz, p->Kp);
   if ((rc = after_launch(ctx, "gather_coords_kernel"))) return rc;
-  pattern_norm_kernel<<<ceil_div(N, 128), 128, 0, ctx->stream>>>(d_images, d_mask, n2, N,
-                                                                 p->d.normalize_images, p->cnorm);
-  if ((rc = after_launch(ctx, "pattern_norm_kernel"))) return rc;
-  // Kt / K2 exist only for the FP32 path (null: not written).
-  pattern_ops_kernel<<<dim3(ceil_div(p->Kp, 256), N), 256, 0, ctx->stream>>>(
-      d_images, p->pix, p->cnorm, n2, N, p->Kp, p->Kraw, p->Kt, p->K2, p->flags);
-  if ((rc = after_launch(ctx, "pattern_ops_kernel"))) return rc;
-  row_sum_kernel<<<N, 256, 0, ctx->stream>>>(p->Kraw, p->Kp, p->Kp, p->Ksum);
-  if ((rc = after_launch(ctx, "row_sum_kernel"))) return rc;
+  p->images = d_images;
+  p->mask = d_mask;
+  if ((rc = pattern_side(p, nullptr, false))) return rc;
   int hflags[16];
   EMC_CUDA(ctx, cudaMemcpyAsync(hflags, p->flags, sizeof(hflags), cudaMemcpyDeviceToHost, ctx->stream));
   EMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
@@ -1031,6 +1067,9 @@ extern "C" int emc_plan_bind(emc_plan* p, const float* d_images, const int* d_ma
   if (p->d.precision == EMC_PREC_MIXED) {
     if ((rc = tc_bind(p))) return rc;
   }
+  // with pruning on, a new binding starts from the input pattern order, the
+  // coherent order of its own rotations and a full scan
+  if ((rc = prune_reset(p))) return rc;
   p->bound = true;
   return EMC_OK;
 }
@@ -1129,6 +1168,11 @@ static int iterate_enqueue(emc_plan* p, float* d_model, float* d_weight) {
   };
   if ((rc = mark(0))) return rc;
   EMC_CUDA(ctx, cudaMemsetAsync(p->flags + 4, 0, sizeof(int), ctx->stream));
+  if (p->prune_tiles) {  // skipped tiles contribute (max, sum exp) = (-inf, 0)
+    fill_part_kernel<<<ctx->sm_count * 4, 256, 0, ctx->stream>>>(p->part,
+                                                                (size_t)p->n_rt * N);
+    if ((rc = after_launch(ctx, "fill_part_kernel"))) return rc;
+  }
   // expand
   if ((rc = plan_expand(p, d_model))) return rc;
   if ((rc = mark(1))) return rc;
@@ -1153,7 +1197,7 @@ static int iterate_enqueue(emc_plan* p, float* d_model, float* d_weight) {
   mprep_kernel<<<R, kMprepThreads, stage ? sizeof(float) * N : 0, ctx->stream>>>(
       p->L, p->PHI, p->lse2, p->Ksum, p->cnorm, R, N, tcm ? nullptr : p->Q,
       tcm ? p->Qh : nullptr, tcm ? p->Ql : nullptr, p->qscale, p->Np, p->T, row_mass, row_bound,
-      stage);
+      stage, p->prune_tiles ? p->prune_state : nullptr, p->n_rt, p->prune_margin);
   if ((rc = after_launch(ctx, "mprep_kernel"))) return rc;
   if ((rc = mark(4))) return rc;
   // M-step into zeroed accumulators
@@ -1257,6 +1301,11 @@ extern "C" int emc_plan_wait(emc_plan* p, emc_iter_stats* stats) {
 
 extern "C" int emc_iterate(emc_plan* p, float* d_model, float* d_weight, float sigma,
                            emc_iter_stats* stats) {
+  if (p && p->prune) {
+    bool handled = false;
+    const int prc = prune_iterate(p, d_model, d_weight, sigma, stats, &handled);
+    if (handled || prc) return prc;
+  }
   int rc = emc_iterate_async(p, d_model, d_weight, sigma);
   if (rc) return rc;
   return emc_plan_wait(p, stats);

@@ -73,6 +73,13 @@ struct emc_plan {
   float* sigma_dev = nullptr;  // [1] annealing width read by the E-step kernels
   emc::BlurWork blur{};        // plan-owned blur buffers and taps (blur_sigma > 0)
 
+  // pruned iteration (prune.cu): set for the iteration being enqueued
+  int2* prune_tiles = nullptr;          // (pattern tile, rotation tile) list, device
+  int prune_n_tiles = 0;
+  unsigned char* prune_state = nullptr; // [n_pt][n_rt] 0 skipped, 1 evaluated, 2 margin
+  double* prune_margin = nullptr;       // [R] responsibility mass in margin tiles
+  void* prune = nullptr;                // PruneState
+
   // one captured iteration (emc_plan_capture / emc_plan_replay)
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t graph_exec = nullptr;
@@ -108,6 +115,12 @@ int plan_alloc(emc_plan* p, void** ptr, size_t bytes);
 
 // Tensor-core path (tc_gemm.cu).
 int tc_bind(emc_plan* p);
+int prune_iterate(emc_plan* p, float* model, float* weight, float sigma, emc_iter_stats* stats,
+                  bool* handled);
+void prune_free(emc_plan* p);
+int prune_reset(emc_plan* p);
+int tc_pattern_side(emc_plan* p, const int* d_perm);
+int pattern_side(emc_plan* p, const int* d_perm, bool with_tc);
 int tc_estep(emc_plan* p);
 int tc_mstep(emc_plan* p, float* model, float* weight);
 int* tc_status(emc_plan* p);  // device status word of the tensor-core pipelines

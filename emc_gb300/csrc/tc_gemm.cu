@@ -88,14 +88,15 @@ constexpr float kMSScale = 1.0f / 256.0f;  // (M' S) * 2^-8 keeps slices below 2
 // Kh = k, K2h + K2l = k^2 * 2^-7 exactly (K2h == nullptr: Kh only).
 __global__ void tc_pattern_ops_kernel(const float* __restrict__ images, const int* __restrict__ pix,
                                       int n2, int N, int Kp, __half* __restrict__ Kh,
-                                      __half* __restrict__ K2h, __half* __restrict__ K2l) {
+                                      __half* __restrict__ K2h, __half* __restrict__ K2l,
+                                      const int* __restrict__ perm) {
   const int i = blockIdx.y;
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= Kp) return;
   float k = 0.0f;
   if (i < N) {
     const int p = pix[q];
-    if (p >= 0) k = __ldg(images + (size_t)i * n2 + p);
+    if (p >= 0) k = __ldg(images + (size_t)(perm ? perm[i] : i) * n2 + p);
   }
   const float k2 = k * k * kK2Scale;  // exact: k^2 < 2^22
   const __half hi = __float2half_rn(k2);
@@ -209,6 +210,7 @@ constexpr int GROUP = 8;       // rotation tiles per raster group
 struct TcEstepArgs {
   int N, R, Kp, n_pt, n_rt, nkb;
   int gh_lo;                      // 1: G and H as FP16 hi + lo, 0: hi only
+  const int2* tiles;              // pruned iteration: (pattern tile, rotation tile) per CTA
   const unsigned char* k2lo_any;  // [n_pt][nkb]
   const float* rot_cnt;
   const float* rot_A;
@@ -243,13 +245,19 @@ __global__ void __launch_bounds__(es::THREADS, 1)
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const float sg = *a.sigma;
   const float inv2s2 = 1.0f / (2.0f * sg * sg);
-  // grouped raster: GROUP rotation tiles share each pattern tile in turn
-  const int per_group = GROUP * a.n_pt;
-  const int g = blockIdx.x / per_group, within = blockIdx.x % per_group;
-  const int rt0 = g * GROUP;
-  const int gsz = min(GROUP, a.n_rt - rt0);
-  const int rt = rt0 + within % gsz;
-  const int pt = within / gsz;
+  int pt, rt;
+  if (a.tiles) {  // pruned: the listed tiles only
+    const int2 t = a.tiles[blockIdx.x];
+    pt = t.x;
+    rt = t.y;
+  } else {  // grouped raster: GROUP rotation tiles share each pattern tile in turn
+    const int per_group = GROUP * a.n_pt;
+    const int g = blockIdx.x / per_group, within = blockIdx.x % per_group;
+    const int rt0 = g * GROUP;
+    const int gsz = min(GROUP, a.n_rt - rt0);
+    rt = rt0 + within % gsz;
+    pt = within / gsz;
+  }
   const int n0 = pt * BM, r0 = rt * BN;
 
   if (threadIdx.x == 0) {
@@ -411,6 +419,7 @@ constexpr int GROUP = 8;
 
 struct TcEstepPoisArgs {
   int N, R, n_pt, n_rt, nkb;
+  const int2* tiles;      // pruned iteration: (pattern tile, 256-rotation tile) per CTA
   int n_part;             // 128-rotation partial tiles
   const float* rot_ssum;  // S_r
   const float* rotw;
@@ -438,12 +447,19 @@ __global__ void __launch_bounds__(ep::THREADS, 1)
   float* s_lw = s_ss + BN;
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int per_group = GROUP * a.n_pt;
-  const int g = blockIdx.x / per_group, within = blockIdx.x % per_group;
-  const int rt0 = g * GROUP;
-  const int gsz = min(GROUP, a.n_rt - rt0);
-  const int rt = rt0 + within % gsz;
-  const int pt = within / gsz;
+  int pt, rt;
+  if (a.tiles) {  // pruned: the listed tiles only
+    const int2 t = a.tiles[blockIdx.x];
+    pt = t.x;
+    rt = t.y;
+  } else {
+    const int per_group = GROUP * a.n_pt;
+    const int g = blockIdx.x / per_group, within = blockIdx.x % per_group;
+    const int rt0 = g * GROUP;
+    const int gsz = min(GROUP, a.n_rt - rt0);
+    rt = rt0 + within % gsz;
+    pt = within / gsz;
+  }
   const int n0 = pt * BM, r0 = rt * BN;
 
   if (threadIdx.x == 0) {
@@ -887,8 +903,18 @@ int tc_bind(emc_plan* p) {
     EMC_CUDA(ctx, cudaFuncSetAttribute(tc_mstep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        ms::SMEM_BYTES));
   }
+  return tc_pattern_side(p, nullptr);
+}
+
+// FP16 pattern operands for the pattern order perm (position -> input
+// pattern; nullptr: input order).
+int tc_pattern_side(emc_plan* p, const int* d_perm) {
+  emc_ctx* ctx = p->ctx;
+  const int N = p->d.n_images, Np = p->Np, Kp = p->Kp;
+  const bool pois = p->d.diff == EMC_DIFF_TRUE_POISSON;
+  int rc;
   tc_pattern_ops_kernel<<<dim3(ceil_div(Kp, 256), Np), 256, 0, ctx->stream>>>(
-      p->images, p->pix, p->n2, N, Kp, p->Kh, pois ? nullptr : p->K2hi, p->K2lo);
+      p->images, p->pix, p->n2, N, Kp, p->Kh, pois ? nullptr : p->K2hi, p->K2lo, d_perm);
   if ((rc = after_launch(ctx, "tc_pattern_ops_kernel"))) return rc;
   if (!pois) tc_k2lo_flags_kernel<<<dim3(Kp / 32, Np / 128), 256, 0, ctx->stream>>>(p->K2lo, Kp, p->k2lo_any,
                                                                          Kp / 32);
@@ -913,6 +939,7 @@ static int tc_estep_pois(emc_plan* p) {
   a.n_pt = p->Np / ep::BM;
   a.n_rt = ceil_div(p->Rp, ep::BN);
   a.nkb = p->Kp / ep::BK;
+  a.tiles = p->prune_tiles;
   a.n_part = p->n_rt;
   a.rot_ssum = p->rot_ssum;
   a.rotw = p->rotw;
@@ -923,8 +950,10 @@ static int tc_estep_pois(emc_plan* p) {
   a.PHI = p->PHI;
   a.part = p->part;
   a.status = st->status;
-  tc_estep_pois_kernel<<<a.n_pt * a.n_rt, ep::THREADS, ep::SMEM_BYTES, ctx->stream>>>(
-      st->mK, st->mLh, st->mLl, a);
+  const int grid = p->prune_tiles ? p->prune_n_tiles : a.n_pt * a.n_rt;
+  if (grid == 0) return EMC_OK;
+  tc_estep_pois_kernel<<<grid, ep::THREADS, ep::SMEM_BYTES, ctx->stream>>>(st->mK, st->mLh,
+                                                                           st->mLl, a);
   return after_launch(ctx, "tc_estep_pois_kernel");
 }
 
@@ -945,6 +974,7 @@ int tc_estep(emc_plan* p) {
   a.n_rt = p->Rp / es::BN;
   a.nkb = p->Kp / es::BK;
   a.gh_lo = p->estep_gh_lo;
+  a.tiles = p->prune_tiles;
   a.k2lo_any = p->k2lo_any;
   a.rot_cnt = p->rot_cnt;
   a.rot_A = p->rot_A;
@@ -958,7 +988,9 @@ int tc_estep(emc_plan* p) {
   a.bad = p->flags + 4;
   a.status = st->status;
   const CUtensorMap* rm = st->rot;
-  tc_estep_kernel<<<a.n_pt * a.n_rt, es::THREADS, es::SMEM_BYTES, ctx->stream>>>(
+  const int grid = p->prune_tiles ? p->prune_n_tiles : a.n_pt * a.n_rt;
+  if (grid == 0) return EMC_OK;
+  tc_estep_kernel<<<grid, es::THREADS, es::SMEM_BYTES, ctx->stream>>>(
       st->mK, st->mK2h, st->mK2l, rm[0], rm[1], rm[2], rm[3], rm[4], rm[5], a);
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(ctx, e, "tc_estep_kernel launch");

@@ -68,6 +68,7 @@ typedef struct emc_plan emc_plan;
 /* Replaces cuda_set_device (emc_cuda.cu:867-870; main.cpp:127): binds the
  * context to `device` and creates its stream. */
 int emc_ctx_create(emc_ctx** out, int device);
+/* Destroy every plan and batch of a context before the context. */
 int emc_ctx_destroy(emc_ctx* ctx);
 /* Text of the last error on this context (never NULL). */
 const char* emc_last_error(const emc_ctx* ctx);
@@ -330,6 +331,34 @@ int emc_plan_wait(emc_plan* plan, emc_iter_stats* stats);
  * emc_plan_wait for errors and stats.  Re-capture after emc_plan_bind. */
 int emc_plan_capture(emc_plan* plan, float* d_model, float* d_weight);
 int emc_plan_replay(emc_plan* plan, float sigma);
+/* Pruned iterations (no counterpart in the reference; tensor-core path).  With pruning on, every emc_iterate after the first evaluates only
+ * the (128-pattern, 128-rotation) tiles that held more than
+ * (1 - min_mass) / (10 n_rotation_tiles) of some pattern's responsibility in
+ * the previous iteration (patterns re-sorted by their most probable
+ * rotation), plus a margin of the rotation tiles within `dilate`
+ * nearest-neighbour angles of those.  When more than 1 - min_mass of the
+ * mass per pattern falls in the margin, the iteration is repeated from its
+ * input model as a full scan.  Responsibilities outside the evaluated tiles
+ * are 0.  full_every > 0 also makes every full_every-th iteration a full scan
+ * (a check of the pruning against distributions that move beyond the margin
+ * between iterations).  While pruning is on, emc_plan_results is in the plan's pattern
+ * order (emc_plan_pattern_order: position -> input pattern); emc_iterate_async
+ * and the graph forms always run full scans. */
+typedef struct {
+  int pruned;                 /* the last emc_iterate evaluated a tile subset  */
+  int fallback;               /* ... and was then repeated as a full scan      */
+  double active_fraction;     /* evaluated share of the tiles, next iteration   */
+  double core_fraction;       /* ... of which core tiles (before the margin)    */
+  double margin_mass;         /* mass per pattern in margin tiles, last pruned  */
+  double nn_angle;            /* median nearest-neighbour rotation angle (rad)  */
+  long long pruned_iterations, fallback_iterations, full_iterations;
+} emc_prune_info;
+int emc_plan_set_pruning(emc_plan* plan, int on, float min_mass, float dilate, int full_every);
+int emc_plan_prune_info(emc_plan* plan, emc_prune_info* info);
+int emc_plan_pattern_order(emc_plan* plan, int* h_order);
+/* Rotation order of the results while pruning is on (the plan keeps its
+ * rotations in a spatially coherent order): row -> input rotation. */
+int emc_plan_rotation_order(emc_plan* plan, int* h_order);
 /* Batched reconstructions (no counterpart in the reference): n bound plans,
  * each with its own model/weight, captured (emc_plan_capture) and nested as
  * independent child graphs of one graph; emc_batch_run launches one

@@ -62,6 +62,8 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--prune-steps", type=int, default=4,
+                    help="timed iterations of the pruned-vs-full leg (0: skip)")
     return ap.parse_args()
 
 
@@ -331,8 +333,71 @@ def run_ours(args):
     if args.e2e_steps > 0:
         e2e = run_e2e(args, prob, plan, images, mask, x, y, z, rot, w, model, weight, sig,
                       torch_stream, ws, pairs)
+    pruned = None
+    if precision == "mixed" and args.prune_steps > 0 and rank == 0:
+        pruned = prune_leg(args, prob, ctx, T, (images, mask, x, y, z, rot, w), pairs)
     return finish(args, prob, plan, ctx, ws, rank, precision, value, ms_step, st, plain, e2e,
-                  estep_ms, phases, launches, clocks, pairs)
+                  estep_ms, phases, launches, clocks, pairs, pruned)
+
+
+def prune_leg(args, prob, ctx, T, inputs, pairs):
+    """Pruned against full-scan iterations of the counts x log-slice Poisson
+    likelihood (the likelihood whose responsibilities are peaked enough to
+    prune; the reference's sigma-tempered one is not at these sigmas), in the
+    late-iteration regime: both runs start from the state after 3 full
+    iterations begun at the true particle, then run 2 untimed and K timed
+    iterations each.  Reports both throughputs, the evaluated share of the
+    tiles, fallbacks and the final model's distance to the full-scan run."""
+    import numpy as np
+    import torch
+
+    import emc_gb300 as E
+    s, R, N = prob.cfg.side, prob.quats.shape[0], prob.images.shape[0]
+
+    def plan_b():
+        p = E.Plan(ctx, s, N, R, diff=E.DIFF_TRUE_POISSON, precision=E.PREC_MIXED)
+        p.bind(*inputs)
+        return p
+    full = plan_b()
+    m0 = T(prob.true_model)
+    ctx.normalize_model(s, m0)
+    w0 = torch.empty_like(m0)
+    for _ in range(3):
+        full.iterate(m0, w0, 0.12, stats=False)
+    runs = {}
+    for kind in ("full", "pruned"):
+        plan = full if kind == "full" else plan_b()
+        if kind == "pruned":
+            plan.set_pruning(True, min_mass=0.999, dilate=1.0)
+        m = m0.clone()
+        w = torch.empty_like(m)
+        torch.cuda.synchronize()
+        for _ in range(2):
+            plan.iterate(m, w, 0.12, stats=False)
+        t = []
+        for _ in range(args.prune_steps):
+            t0 = time.perf_counter()
+            plan.iterate(m, w, 0.12, stats=False)  # returns after its own synchronise
+            t.append(time.perf_counter() - t0)
+        runs[kind] = (statistics.mean(t), m.cpu().numpy().astype(np.float64),
+                      plan.prune_info() if kind == "pruned" else None)
+        if kind == "pruned":
+            plan.close()
+    full.close()
+    tf, mf, _ = runs["full"]
+    tp, mp, info = runs["pruned"]
+    return {"likelihood": "true poisson (counts x log slice), mixed precision",
+            "state": "after 3 full iterations from the true particle (late-iteration regime)",
+            "timing": "host clock around emc_iterate, which ends with a synchronise",
+            "full_ms_per_step": tf * 1e3, "pruned_ms_per_step": tp * 1e3,
+            "speedup": tf / tp,
+            "full_scan_equivalent_pairs_per_s": pairs / tp,
+            "evaluated_pairs_per_s": pairs * info["active_fraction"] / tp,
+            "active_fraction": info["active_fraction"], "core_fraction": info["core_fraction"],
+            "pruned_iterations": info["pruned_iterations"],
+            "fallback_iterations": info["fallback_iterations"],
+            "full_iterations": info["full_iterations"],
+            "model_rel_l2_vs_full_scan": float(np.linalg.norm(mp - mf) / np.linalg.norm(mf))}
 
 
 def run_e2e(args, prob, plan, images, mask, x, y, z, rot, w, model, weight, sig, torch_stream, ws,
@@ -367,7 +432,7 @@ def run_e2e(args, prob, plan, images, mask, x, y, z, rot, w, model, weight, sig,
 
 
 def finish(args, prob, plan, ctx, ws, rank, precision, value, ms_step, st, plain, e2e, estep_ms,
-           phases, launches, clocks, pairs):
+           phases, launches, clocks, pairs, pruned=None):
     # ---- roofline of the dominant kernel (E-step)
     peaks = load_peaks()
     p_eff = int(prob.mask.sum())
@@ -409,6 +474,7 @@ def finish(args, prob, plan, ctx, ws, rank, precision, value, ms_step, st, plain
                            mstep_atomics="warp-aggregated" if args.mstep_aggregate else "per pair"),
             "iter_per_s": ws * 1e3 / ms_step,
             "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "plain_fp32": plain,
+            "pruned": pruned,
             "speedup_vs_plain_fp32": (plain["ms_per_step"] / ms_step) if plain else None,
             "phase_ms": phase_mean, "gpu_launches": launches, "clocks": clocks,
             "total_loglik": st.total_loglik, "captured_mass": st.captured_mass,

@@ -78,6 +78,8 @@ struct emc_plan {
   int prune_n_tiles = 0;
   unsigned char* prune_state = nullptr; // [n_pt][n_rt] 0 skipped, 1 evaluated, 2 margin
   double* prune_margin = nullptr;       // [R] responsibility mass in margin tiles
+  int* prune_kb_off = nullptr;          // [n_rt + 1] M-step k-blocks per rotation tile
+  int* prune_kb_list = nullptr;         // the 64-pattern k-blocks themselves
   void* prune = nullptr;                // PruneState
 
   // one captured iteration (emc_plan_capture / emc_plan_replay)

@@ -42,6 +42,7 @@ struct PruneState {
   unsigned char *d_core = nullptr, *d_state = nullptr, *d_adj = nullptr;
   int2* d_tiles = nullptr;
   int n_tiles = 0;
+  int *d_kb_off = nullptr, *d_kb_list = nullptr;  // M-step k-blocks per rotation tile
   float* d_model_in = nullptr;
   float* d_nn = nullptr;
   // rotation order: internal row -> input rotation, and the input buffers
@@ -162,6 +163,8 @@ static int prune_alloc(emc_plan* p, PruneState* ps) {
   if (!rc) rc = plan_alloc(p, (void**)&ps->d_model_in, sizeof(float) * n3);
   if (!rc) rc = plan_alloc(p, (void**)&ps->d_margin, sizeof(double) * (size_t)R);
   if (!rc) rc = plan_alloc(p, (void**)&ps->d_nn, sizeof(float) * (size_t)R);
+  if (!rc) rc = plan_alloc(p, (void**)&ps->d_kb_off, sizeof(int) * ((size_t)n_rt + 1));
+  if (!rc) rc = plan_alloc(p, (void**)&ps->d_kb_list, sizeof(int) * 2 * (size_t)n_pt * n_rt);
   if (!rc) rc = plan_alloc(p, (void**)&ps->d_rot, sizeof(float) * 4 * (size_t)R);
   if (!rc) rc = plan_alloc(p, (void**)&ps->d_rotw, sizeof(float) * (size_t)R);
   return rc;
@@ -317,6 +320,22 @@ static int prune_prepare(emc_plan* p, PruneState* ps, bool reorder) {
         }
   ps->n_tiles = (int)tiles.size();
   ps->info.active_fraction = (double)rows / ((double)n_pt * n_rt);
+  // M-step: per rotation tile, the 64-pattern k-blocks of its evaluated pattern tiles
+  std::vector<int> kb_off(n_rt + 1), kb_list;
+  for (int rt = 0; rt < n_rt; ++rt) {
+    kb_off[rt] = (int)kb_list.size();
+    for (int pt = 0; pt < n_pt; ++pt)
+      if (state[(size_t)pt * n_rt + rt]) {
+        kb_list.push_back(2 * pt);
+        kb_list.push_back(2 * pt + 1);
+      }
+  }
+  kb_off[n_rt] = (int)kb_list.size();
+  EMC_CUDA(ctx, cudaMemcpyAsync(ps->d_kb_off, kb_off.data(), sizeof(int) * (n_rt + 1),
+                                cudaMemcpyHostToDevice, ctx->stream));
+  if (!kb_list.empty())
+    EMC_CUDA(ctx, cudaMemcpyAsync(ps->d_kb_list, kb_list.data(), sizeof(int) * kb_list.size(),
+                                  cudaMemcpyHostToDevice, ctx->stream));
   ps->info.core_fraction =
       (double)std::count(state.begin(), state.end(), (unsigned char)1) / ((double)n_pt * n_rt);
   if (!tiles.empty())
@@ -378,11 +397,15 @@ int prune_iterate(emc_plan* p, float* model, float* weight, float sigma, emc_ite
   p->prune_n_tiles = ps->n_tiles;
   p->prune_state = ps->d_state;
   p->prune_margin = ps->d_margin;
+  p->prune_kb_off = ps->d_kb_off;
+  p->prune_kb_list = ps->d_kb_list;
   rc = emc_iterate_async(p, model, weight, sigma);
   p->prune_tiles = nullptr;
   p->prune_n_tiles = 0;
   p->prune_state = nullptr;
   p->prune_margin = nullptr;
+  p->prune_kb_off = nullptr;
+  p->prune_kb_list = nullptr;
   if (rc) return rc;
   if ((rc = emc_plan_wait(p, stats))) return rc;
   std::vector<double> margin(R);

@@ -609,8 +609,20 @@ struct TcMstepArgs {
   float2* acc2;
   const double* bounds;
   int q_lo;  // 1: Q hi + lo, 0: Q hi only
+  // pruned iteration: the pattern k-blocks of rotation tile rt are
+  // kb_list[kb_off[rt] .. kb_off[rt+1]) (Q is zero elsewhere); nullptr: all
+  const int* kb_off;
+  const int* kb_list;
   int* status;
 };
+
+// The k-blocks of rotation tile rt: count, and the j-th of them.
+__device__ __forceinline__ int ms_nkb(const TcMstepArgs& a, int rt) {
+  return a.kb_off ? a.kb_off[rt + 1] - a.kb_off[rt] : a.nkb;
+}
+__device__ __forceinline__ int ms_kb(const TcMstepArgs& a, int rt, int j) {
+  return a.kb_off ? a.kb_list[a.kb_off[rt] + j] : j;
+}
 
 __device__ __forceinline__ double tc_fixed_scale(double b) {
   return b > 0.0 ? 2305843009213693952.0 / b : 1.0;
@@ -737,7 +749,9 @@ __global__ void __launch_bounds__(ms::THREADS, 1)
       for (int t = blockIdx.x; t < a.n_tiles && ok; t += gridDim.x) {
         int r0, q0;
         ms_tile(a, t, r0, q0);
-        for (int kb = 0; kb < a.nkb; ++kb, ++it) {
+        const int nk = ms_nkb(a, r0 / BM);
+        for (int j = 0; j < nk; ++j, ++it) {
+          const int kb = ms_kb(a, r0 / BM, j);
           const int s = it % STAGES;
           const uint32_t ph = (it / STAGES) & 1;
           if (!ptx::mbar_wait(&empty[s], ph ^ 1, a.status, 4)) {
@@ -764,7 +778,12 @@ __global__ void __launch_bounds__(ms::THREADS, 1)
         const uint32_t d = tmem + (uint32_t)(b * BN);
         if (!ptx::mbar_wait(&tempty[b], ((j >> 1) & 1) ^ 1, a.status, 7)) break;
         ptx::tc_fence_after();
-        for (int kb = 0; kb < a.nkb; ++kb, ++it) {
+        int r0t, q0t;
+        ms_tile(a, t, r0t, q0t);
+        // a tile with no k-block leaves the buffer as it was: its rotations
+        // have no responsibility (T_r = 0), so the epilogue inserts nothing
+        const int nk = ms_nkb(a, r0t / BM);
+        for (int kb = 0; kb < nk; ++kb, ++it) {
           const int s = it % STAGES;
           const uint32_t ph = (it / STAGES) & 1;
           if (!ptx::mbar_wait(&full[s], ph, a.status, 5)) {
@@ -1024,6 +1043,8 @@ int tc_mstep(emc_plan* p, float* model, float* weight) {
   a.acc2 = p->acc2;
   a.q_lo = p->mstep_q_lo;
   a.aggregate = p->mstep_aggregate;
+  a.kb_off = p->prune_kb_off;
+  a.kb_list = p->prune_kb_list;
   a.bounds = p->red + kRedBoundM;
   a.status = st->status;
   a.n_tiles = a.n_qt * a.n_rt;

@@ -49,15 +49,16 @@ def parse():
     ap.add_argument("--config", default="mid")
     ap.add_argument("--precision", choices=["auto", "mixed", "fp32"], default="auto")
     ap.add_argument("--insert", choices=["atomic", "deterministic"], default="atomic")
-    ap.add_argument("--mstep-qlo", type=int, choices=[0, 1], default=1,
+    ap.add_argument("--mstep-qlo", type=int, choices=[0, 1], default=0,
                     help="tensor M-step: responsibility x scaling as FP16 hi+lo (1) or hi (0)")
     ap.add_argument("--diff", choices=["poisson", "true_poisson"], default="poisson",
                     help="likelihood: the reference's poisson (weighted least squares) or "
                          "the counts x log-slice Poisson likelihood")
     ap.add_argument("--mstep-aggregate", type=int, choices=[0, 1], default=0,
                     help="tensor M-step: warp-aggregated atomics for nearest insertion")
-    ap.add_argument("--estep-ghlo", type=int, choices=[0, 1], default=1,
-                    help="tensor E-step: rotation-side factors as FP16 hi+lo (1) or hi (0)")
+    ap.add_argument("--estep-ghlo", type=int, choices=[-1, 0, 1, 2, 3], default=-1,
+                    help="tensor E-step: lo terms of G (bit 0) and H (bit 1); -1: the library's "
+                         "default (G, and H when the intensity is known)")
     ap.add_argument("--plain-steps", type=int, default=2)
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
@@ -470,7 +471,9 @@ def finish(args, prob, plan, ctx, ws, rank, precision, value, ms_step, st, plain
                            diff="poisson (reference)" if args.diff == "poisson"
                            else "true poisson (counts x log slice)",
                            mstep_q="fp16 hi+lo" if args.mstep_qlo else "fp16 hi",
-                           estep_gh="fp16 hi+lo" if args.estep_ghlo else "fp16 hi",
+                           estep_gh={-1: "G fp16 hi+lo, H fp16 hi", 3: "G, H fp16 hi+lo",
+                                     2: "G hi, H hi+lo", 1: "G hi+lo, H hi",
+                                     0: "G, H fp16 hi"}[args.estep_ghlo],
                            mstep_atomics="warp-aggregated" if args.mstep_aggregate else "per pair"),
             "iter_per_s": ws * 1e3 / ms_step,
             "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "plain_fp32": plain,

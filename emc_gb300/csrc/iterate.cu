@@ -1438,7 +1438,7 @@ extern "C" int emc_plan_set_option(emc_plan* p, int option, int value) {
   if (!p) return EMC_ERR_INVALID;
   emc_ctx* ctx = p->ctx;
   if (option == EMC_OPT_ESTEP_GHLO) {
-    EMC_REQUIRE(ctx, value == 0 || value == 1, "plan_set_option: gh_lo %d", value);
+    EMC_REQUIRE(ctx, value >= -1 && value <= 3, "plan_set_option: gh_lo %d", value);
     p->estep_gh_lo = value;
     return EMC_OK;
   }

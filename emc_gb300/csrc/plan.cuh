@@ -92,8 +92,8 @@ struct emc_plan {
   cudaEvent_t ev[kPhases + 1] = {};
 
   void* tc = nullptr;  // tensor-core state (tensor maps, rotation operands)
-  int estep_gh_lo = 1;    // tensor E-step: G, H as FP16 hi + lo (1) or hi only (0)
-  int mstep_q_lo = 1;     // tensor M-step: Q as FP16 hi + lo (1) or hi only (0)
+  int estep_gh_lo = -1;   // tensor E-step lo terms: bit 0 G, bit 1 H; -1 auto
+  int mstep_q_lo = 0;     // tensor M-step: Q as FP16 hi + lo (1) or hi only (0)
   int mstep_aggregate = 0;  // tensor M-step: warp-aggregated float atomics (nearest)
 
   std::vector<void*> allocs;

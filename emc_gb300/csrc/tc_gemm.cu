@@ -209,7 +209,7 @@ constexpr int GROUP = 8;       // rotation tiles per raster group
 
 struct TcEstepArgs {
   int N, R, Kp, n_pt, n_rt, nkb;
-  int gh_lo;                      // 1: G and H as FP16 hi + lo, 0: hi only
+  int gh_lo;                      // lo terms: bit 0 G, bit 1 H (3: both, 0: hi only)
   const int2* tiles;              // pruned iteration: (pattern tile, rotation tile) per CTA
   const unsigned char* k2lo_any;  // [n_pt][nkb]
   const float* rot_cnt;
@@ -284,7 +284,7 @@ __global__ void __launch_bounds__(es::THREADS, 1)
   ptx::tc_fence_after();
   const uint32_t tmem = *tmem_slot;
   const unsigned char* flags = a.k2lo_any + (size_t)pt * a.nkb;
-  const bool ghlo = a.gh_lo != 0;
+  const bool glo = (a.gh_lo & 1) != 0, hlo = (a.gh_lo & 2) != 0;
 
   if (warp == 0) {
     // ------------------------------------------------ TMA producer
@@ -295,12 +295,12 @@ __global__ void __launch_bounds__(es::THREADS, 1)
         const uint32_t ph = (kb / STAGES) & 1;
         if (!ptx::mbar_wait(&empty[s], ph ^ 1, a.status, 0)) break;
         const bool lo = flags[kb] != 0;
-        const int ntiles = kSlots - (lo ? 0 : 1) - (ghlo ? 0 : 2);
+        const int ntiles = kSlots - (lo ? 0 : 1) - (glo ? 0 : 1) - (hlo ? 0 : 1);
         ptx::mbar_arrive_expect_tx(&full[s], ntiles * TILE_BYTES);
         unsigned char* st = smem + s * STAGE_BYTES;
         for (int j = 0; j < kSlots; ++j) {
           if (j == sK2l && !lo) continue;
-          if ((j == sGl || j == sHl) && !ghlo) continue;
+          if ((j == sGl && !glo) || (j == sHl && !hlo)) continue;
           ptx::tma_load_2d(st + j * TILE_BYTES, maps[j], kb * BK, j < sGh ? n0 : r0, &full[s]);
         }
       }
@@ -325,10 +325,8 @@ __global__ void __launch_bounds__(es::THREADS, 1)
           const uint32_t acc = (kb | ks) ? 1u : 0u;
           ptx::mma_f16(tmem + 0, d(sK), d(sGh), idesc2, acc);      // B hi | den
           ptx::mma_f16(tmem + 256, d(sK2h), d(sHh), idesc2, acc);  // C hi | num
-          if (ghlo) {
-            ptx::mma_f16(tmem + 0, d(sK), d(sGl), idesc1, 1u);     // B lo
-            ptx::mma_f16(tmem + 256, d(sK2h), d(sHl), idesc1, 1u); // C lo
-          }
+          if (glo) ptx::mma_f16(tmem + 0, d(sK), d(sGl), idesc1, 1u);     // B lo
+          if (hlo) ptx::mma_f16(tmem + 256, d(sK2h), d(sHl), idesc1, 1u); // C lo
           if (lo) ptx::mma_f16(tmem + 256, d(sK2l), d(sHh), idesc2, 1u);  // K^2 lo: C | num
         }
         ptx::mma_commit(&empty[s]);
@@ -992,7 +990,9 @@ int tc_estep(emc_plan* p) {
   a.n_pt = p->Np / es::BM;
   a.n_rt = p->Rp / es::BN;
   a.nkb = p->Kp / es::BK;
-  a.gh_lo = p->estep_gh_lo;
+  // auto: G lo always; H lo too when the intensity is known (phi = 1 leaves
+  // the C = K^2 . H term unbalanced, and its rounding shows in the likelihood)
+  a.gh_lo = p->estep_gh_lo >= 0 ? p->estep_gh_lo : (p->d.known_intensity ? 3 : 1);
   a.tiles = p->prune_tiles;
   a.k2lo_any = p->k2lo_any;
   a.rot_cnt = p->rot_cnt;

@@ -372,13 +372,15 @@ int emc_batch_run(emc_batch* batch, const float* sigmas);
 int emc_batch_wait(emc_batch* batch, emc_iter_stats* stats);
 int emc_batch_destroy(emc_batch* batch);
 /* Precision knobs of the tensor-core kernels.
- * EMC_OPT_ESTEP_GHLO: 1 (default) takes the likelihood's rotation-side
- * factors s/(s+c) and 1/(s+c) as FP16 hi + lo, 0 as FP16 hi only (4 instead
- * of 6 MMAs per 16-pixel step, ~2^-12 relative rounding per factor). */
+ * EMC_OPT_ESTEP_GHLO: which of the likelihood's rotation-side factors
+ * G = s/(s+c) (bit 0) and H = 1/(s+c) (bit 1) carry an FP16 lo term besides
+ * their FP16 hi term (one 128-column MMA per 16-pixel step each, ~2^-12
+ * relative rounding of a factor without it).  -1 (default): G always, H too
+ * when known_intensity fixes the scaling at 1; 0..3 set the bits. */
 #define EMC_OPT_ESTEP_GHLO 3
-/* EMC_OPT_MSTEP_QLO: 1 (default) multiplies responsibility/scaling as FP16
- * hi + lo, 0 as FP16 hi only (half the M-step MMAs, ~2^-12 relative
- * rounding per term). */
+/* EMC_OPT_MSTEP_QLO: 0 (default) multiplies responsibility/scaling as FP16
+ * hi only (~2^-12 relative rounding per term), 1 as FP16 hi + lo (twice the
+ * M-step MMAs). */
 #define EMC_OPT_MSTEP_QLO 2
 /* EMC_OPT_MSTEP_AGGREGATE: 1 combines, inside each warp, the nearest-voxel
  * insertions that land on the same voxel before one atomic (float atomics

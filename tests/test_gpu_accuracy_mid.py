@@ -42,10 +42,13 @@ def oracle_run(prob):
     return models, lls
 
 
+# mixed: the defaults (G hi + lo, H hi, Q hi); mixed-hilo: every factor hi + lo;
+# mixed-hi: every factor hi only (close to the log-likelihood target: the G lo
+# term matters, the H and Q lo terms do not)
 @pytest.mark.parametrize("precision,q_lo,gh_lo",
-                         [(E.PREC_FP32, 1, 1), (E.PREC_MIXED, 1, 1), (E.PREC_MIXED, 0, 1),
+                         [(E.PREC_FP32, 1, -1), (E.PREC_MIXED, 0, -1), (E.PREC_MIXED, 1, 3),
                           (E.PREC_MIXED, 0, 0)],
-                         ids=["fp32", "mixed", "mixed-qhi", "mixed-hi"])
+                         ids=["fp32", "mixed", "mixed-hilo", "mixed-hi"])
 def test_mid_geometry_accuracy(ctx, cuda, prob, oracle_run, precision, q_lo, gh_lo):
     want_models, want_lls = oracle_run
     s, R, N = prob.cfg.side, prob.quats.shape[0], prob.images.shape[0]

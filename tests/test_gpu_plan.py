@@ -71,6 +71,9 @@ MIXED_CASES = [
     # FP16 hi-only rotation-side factors and M-step operand
     (dict(interp=E.INTERP_NEAREST, options={E.Plan.OPT_ESTEP_GHLO: 0, E.Plan.OPT_MSTEP_QLO: 0}),
      True),
+    # every factor hi + lo
+    (dict(interp=E.INTERP_NEAREST, options={E.Plan.OPT_ESTEP_GHLO: 3, E.Plan.OPT_MSTEP_QLO: 1}),
+     True),
 ]
 # tolerances: (log-likelihood rel, scaling rel, model rel L2, respons abs)
 TOL = {E.PREC_FP32: (1e-5, 1e-5, 1e-4, 1e-4), E.PREC_MIXED: (2e-5, 5e-4, 5e-4, 1e-3)}

@@ -63,6 +63,9 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ref-gpu-chunk", type=int, default=256,
+                    help="--impl reference: rotations per timed chunk of the reference's own "
+                         "CUDA kernels (0: skip them)")
     ap.add_argument("--prune-steps", type=int, default=4,
                     help="timed iterations of the pruned-vs-full leg (0: skip)")
     return ap.parse_args()
@@ -509,14 +512,103 @@ def run_reference(args):
             vals.append(info["value"])
     v = statistics.mean(vals)
     R, N = prob.quats.shape[0], prob.images.shape[0]
+    ref_gpu = None
+    if dev == "cuda" and args.ref_gpu_chunk > 0:
+        ref_gpu = ref_gpu_leg(prob, args.ref_gpu_chunk)
     line = {"metric": METRIC, "impl": "reference", "value": v, "unit": UNIT, "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": R * N / v * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32/f64",
             "data": "synthetic (seeded; shapes of the mid-size configuration)",
             "config": workload_desc(prob, "reference (quirk-exact CPU restatement)", "sequential"),
             "cpu_baseline": {**info, "value": v},
-            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "reference_gpu": ref_gpu}
     print(json.dumps(line), flush=True)
+
+
+def ref_gpu_leg(prob, chunk):
+    """The reference's own CUDA kernels (emc_cuda.cu, emc_atomic.cu compiled
+    unchanged for sm_103a by oracle/build_ref.sh --kernels) on one chunk of
+    `chunk` rotations x all patterns of the workload, in main.cpp's order for
+    one chunk: slices, scaling, slices, likelihood, max, sum exp, normalise,
+    slices + insertion.  Each reference call synchronises, as it does in the
+    reference.  Returns pairs/s and the full-iteration time it implies."""
+    import ctypes as C
+
+    import numpy as np
+    import torch
+    env = dict(os.environ)
+    if "EMC_REF_DIR" not in env and not os.path.exists("/root/reference/emc_cuda.cu"):
+        env["EMC_REF_DIR"] = os.path.join(ROOT, "baseline", "_ref", "src")
+    so = os.path.join(ROOT, "oracle", "_ref", "libemc_ref_kernels.so")
+    if not os.path.exists(so):
+        r = subprocess.run(["bash", os.path.join(ROOT, "oracle", "build_ref.sh"), "--kernels"],
+                           env=env, capture_output=True, text=True)
+        if r.returncode != 0 or not os.path.exists(so):
+            tail = (r.stderr or r.stdout).strip().splitlines()[-1:] or ["no output"]
+            return {"unavailable": f"reference kernels did not build: {tail[0][:200]}"}
+    lib = C.CDLL(so)
+    dev = torch.device("cuda:0")
+    s, N = prob.cfg.side, prob.images.shape[0]
+    R = prob.quats.shape[0]
+    n2 = s * s
+    chunk = min(chunk, R)
+    T = lambda a, dt=torch.float32: torch.as_tensor(np.ascontiguousarray(a), dtype=dt, device=dev)
+    ptr = lambda t: C.c_void_p(t.data_ptr())
+    model, x, y, z = T(prob.init_model), T(prob.x), T(prob.y), T(prob.z)
+    rot, w = T(prob.quats[:chunk]), T(prob.weights[:chunk])
+    images, mask = T(prob.images), T(prob.mask, torch.int32)
+    slices = torch.empty((chunk, n2), device=dev)
+    scaling = torch.ones((chunk, N), device=dev)
+    respons = torch.empty((chunk, N), device=dev)
+    maxr, sums = torch.empty(N, device=dev), torch.empty(N, device=dev)
+    active = torch.ones(N, dtype=torch.int32, device=dev)
+    new_model, weight = torch.zeros_like(model), torch.zeros_like(model)
+    sigma = C.c_float(0.4)
+    steps = []
+
+    def one():
+        t = {}
+        def timed(name, fn):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            rc = fn()
+            torch.cuda.synchronize()
+            t[name] = t.get(name, 0.0) + (time.perf_counter() - t0)
+            if rc:
+                raise RuntimeError(f"reference {name} returned {rc}")
+        sl = lambda: lib.ref_get_slices(ptr(model), s, ptr(slices), ptr(rot), ptr(x), ptr(y),
+                                        ptr(z), 0, chunk)
+        timed("get_slices", sl)
+        timed("update_scaling_full", lambda: lib.ref_update_scaling_full(
+            ptr(images), ptr(slices), ptr(mask), ptr(scaling), n2, N, 0, chunk, 1))
+        timed("get_slices", sl)
+        timed("calculate_responsabilities", lambda: lib.ref_calculate_responsabilities(
+            ptr(slices), ptr(images), ptr(mask), sigma, ptr(scaling), ptr(respons), ptr(w), n2, N,
+            0, chunk, 1))
+        timed("max_vector", lambda: lib.ref_max_vector(ptr(respons), N, chunk, ptr(maxr)))
+        timed("respons_max_expf", lambda: lib.ref_respons_max_expf(ptr(respons), ptr(maxr), N,
+                                                                   chunk, ptr(sums)))
+        timed("norm_respons_sumexpf", lambda: lib.ref_norm_respons_sumexpf(
+            ptr(respons), ptr(sums), ptr(maxr), N, chunk))
+        timed("get_slices", sl)
+        timed("update_slices", lambda: lib.ref_update_slices(
+            ptr(images), ptr(slices), ptr(mask), ptr(respons), ptr(scaling), ptr(active), N, 0,
+            chunk, n2, s, ptr(new_model), ptr(x), ptr(y), ptr(z), ptr(rot), ptr(weight)))
+        return t
+
+    one()  # warm-up (module load, first launches)
+    for _ in range(2):
+        steps.append(one())
+    per = {k: statistics.mean(st[k] for st in steps) for k in steps[0]}
+    total = sum(per.values())
+    pairs = float(chunk) * N
+    return {"kind": "the reference's CUDA kernels, built unchanged for sm_103a",
+            "sample": f"{chunk} rotations x {N} patterns of the workload, one pass of main.cpp's "
+                      "per-chunk sequence, host clock around each synchronising call",
+            "pairs_per_s": pairs / total, "ms_per_chunk": total * 1e3,
+            "ms_per_call": {k: v * 1e3 for k, v in per.items()},
+            "full_iteration_ms_implied": R * N / (pairs / total) * 1e3}
 
 
 # (side, patterns, rotation level) of the eight batched reconstructions

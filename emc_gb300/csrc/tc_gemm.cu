@@ -202,8 +202,9 @@ constexpr int TILE_BYTES = 128 * BK * 2;  // 8 KB, both operand sides
 // stage slots: pattern side, then the two N=256 pairs, then the lo terms
 enum Slot { sK = 0, sK2h, sK2l, sGh, sMS, sHh, sMp, sGl, sHl, kSlots };
 constexpr int STAGE_BYTES = kSlots * TILE_BYTES;
-constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 4096 + 1024;
-constexpr int EPI_WARPS = 8;   // two per TMEM lane quarter, 64 columns each
+constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 8192 + 1024;  // barriers, row data, parts
+constexpr int EPI_WARPS = 16;  // four per TMEM lane quarter, 32 columns each
+constexpr int EPI_PARTS = EPI_WARPS / 4;
 constexpr int THREADS = 64 + 32 * EPI_WARPS;
 constexpr int GROUP = 8;       // rotation tiles per raster group
 }  // namespace es
@@ -242,7 +243,7 @@ __global__ void __launch_bounds__(es::THREADS, 1)
   float* s_A = (float*)(smem + STAGES * STAGE_BYTES + 256);
   float* s_scale = s_A + BN;
   float* s_lw = s_scale + BN;
-  float2* s_half = (float2*)(s_lw + BN);  // [BM] (max, sum exp) of the second column half
+  float2* s_half = (float2*)(s_lw + BN);  // [EPI_PARTS-1][BM] (max, sum exp) of column parts 1..
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const float sg = *a.sigma;
@@ -339,10 +340,10 @@ __global__ void __launch_bounds__(es::THREADS, 1)
     }
   } else {
     // ------------------------------------------------ epilogue (warps 2-9)
-    // two warps per TMEM lane quarter, each on half of the 128 columns, so
-    // that the expf / divide latency of one hides behind the other
+    // EPI_PARTS warps per TMEM lane quarter, each on a part of the 128
+    // columns, so that the expf / divide latency of one hides behind another
     const int quarter = warp & 3;  // TMEM lanes this warp may access
-    const int half = (warp - 2) >> 2;
+    const int half = (warp - 2) >> 2;  // column part
     const int row = quarter * 32 + lane;
     const int n = n0 + row;
     const bool nok = n < a.N;
@@ -352,7 +353,7 @@ __global__ void __launch_bounds__(es::THREADS, 1)
     if (ptx::mbar_wait(accum, 0, a.status, 2)) {
       ptx::tc_fence_after();
       const uint32_t lane_addr = tmem + ((uint32_t)(quarter * 32) << 16);
-      for (int c0 = half * (BN / 2); c0 < (half + 1) * (BN / 2); c0 += 16) {
+      for (int c0 = half * (BN / EPI_PARTS); c0 < (half + 1) * (BN / EPI_PARTS); c0 += 16) {
         float vn[16], vd[16], vb[16], vc[16];
         ptx::tmem_ld16(lane_addr + 0 + c0, vb);
         ptx::tmem_ld16(lane_addr + 128 + c0, vd);
@@ -389,14 +390,20 @@ __global__ void __launch_bounds__(es::THREADS, 1)
         }
       }
     }
-    // combine the two halves' (max, sum exp) of each row
-    if (half == 1) s_half[row] = make_float2(m, ssum);
+    // combine the parts' (max, sum exp) of each row
+    if (half > 0) s_half[(half - 1) * BM + row] = make_float2(m, ssum);
     asm volatile("bar.sync 1, %0;" ::"n"(EPI_WARPS * 32) : "memory");  // epilogue warps only
     if (half == 0) {
-      const float2 o = s_half[row];
-      const float M = fmaxf(m, o.x);
+      float M = m;
+      for (int q = 1; q < EPI_PARTS; ++q) M = fmaxf(M, s_half[(q - 1) * BM + row].x);
       float S = 0.0f;
-      if (M > -INFINITY) S = ssum * expf(m - M) + o.y * expf(o.x - M);
+      if (M > -INFINITY) {
+        S = ssum * expf(m - M);
+        for (int q = 1; q < EPI_PARTS; ++q) {
+          const float2 o = s_half[(q - 1) * BM + row];
+          S += o.y * expf(o.x - M);
+        }
+      }
       if (nok) a.part[(size_t)rt * a.N + n] = make_float2(M, S);
     }
     if (nbad) atomicAdd(a.bad, nbad);

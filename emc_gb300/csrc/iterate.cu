@@ -578,14 +578,15 @@ __global__ void finite_sum_kernel(const double* __restrict__ x, int n, double* _
 
 // One block per rotation row: P = exp(L - lse) (in place), Q = P / phi,
 // T_r = sum_i P, the row's captured mass and the inserted-mass bound
-// sum_i Q_ri K_i.  Element math is FP32 (expf of an FP64 difference, since
-// FP64 arithmetic is scarce on this GPU); per-thread sums are FP32 and the
-// block sums FP64.
+// sum_i Q_ri K_i.  Element math is FP32 (L - lse with lse as float hi + lo,
+// since FP64 arithmetic is scarce on this GPU); per-thread sums are FP32 and
+// the block sums FP64.
 //   FP32 M-step: Q [R][ldq] (zero padded).
 //   Tensor M-step (Qh != nullptr): Q' = P c_i / phi (phi holds c_i num/den,
-//   the tensor M-step multiplies raw counts) as FP16 hi + lo [R][ldq], each
-//   row scaled by 2^e_r so its largest entry sits near 2^14 (qscale_r =
-//   2^-e_r); the second pass re-reads the row while it is in L2.
+//   the tensor M-step multiplies raw counts) as FP16 hi [R][ldq] (and lo,
+//   when Ql != nullptr), each row scaled by 2^e_r so its largest entry sits
+//   near 2^14 (qscale_r = 2^-e_r); with stage, the row is kept in shared
+//   memory between the two passes, else the second pass re-reads it.
 constexpr int kMprepThreads = 1024;
 constexpr int kMprepStageMax = 30720;  // patterns whose row of Q fits shared memory (120 KB)
 
@@ -664,7 +665,7 @@ __global__ void __launch_bounds__(kMprepThreads) mprep_kernel(
     }
     const __half hi = __float2half_rn(q);
     Qh[(size_t)r * ldq + i] = hi;
-    Ql[(size_t)r * ldq + i] = __float2half_rn(q - __half2float(hi));
+    if (Ql) Ql[(size_t)r * ldq + i] = __float2half_rn(q - __half2float(hi));
   }
   if (threadIdx.x == 0) qscale[r] = ldexpf(1.0f, -ex);
 }
@@ -1196,7 +1197,8 @@ static int iterate_enqueue(emc_plan* p, float* d_model, float* d_weight) {
   const int stage = tcm && N <= kMprepStageMax;
   mprep_kernel<<<R, kMprepThreads, stage ? sizeof(float) * N : 0, ctx->stream>>>(
       p->L, p->PHI, p->lse2, p->Ksum, p->cnorm, R, N, tcm ? nullptr : p->Q,
-      tcm ? p->Qh : nullptr, tcm ? p->Ql : nullptr, p->qscale, p->Np, p->T, row_mass, row_bound,
+      tcm ? p->Qh : nullptr, tcm && p->mstep_q_lo ? p->Ql : nullptr, p->qscale, p->Np, p->T,
+      row_mass, row_bound,
       stage, p->prune_tiles ? p->prune_state : nullptr, p->n_rt, p->prune_margin);
   if ((rc = after_launch(ctx, "mprep_kernel"))) return rc;
   if ((rc = mark(4))) return rc;

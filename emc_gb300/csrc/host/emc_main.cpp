@@ -3,7 +3,13 @@
 // C ABI of libemc_gb300.so.
 //
 //   emc [config] [--dropin] [--precision fp32|mixed] [--deterministic]
-//       [--interp nearest|trilinear] [--out DIR] [--iterations N]
+//       [--interp nearest|trilinear] [--out DIR] [--iterations N] [--graph]
+//       [--prune]
+//
+// --graph records the fused iteration once as a CUDA graph and replays it
+// (emc_plan_capture / emc_plan_replay); --prune turns on pruned iterations
+// (emc_plan_set_pruning, mixed precision), whose debug responsibilities are
+// written back in the input pattern and rotation order.
 //
 // config defaults to ../emc.conf as in main.cpp:66-70.  Inputs replace the
 // reference's HDF5 reads (emc_helper.cpp:198-368, absent libraries) by raw
@@ -53,6 +59,8 @@ struct Opts {
   int insert = EMC_INSERT_ATOMIC;
   int interp = EMC_INTERP_NEAREST;
   int iterations = -1;
+  bool graph = false;
+  bool prune = false;
 };
 
 [[noreturn]] void die(const char* what, const char* detail = "") {
@@ -124,6 +132,8 @@ Opts parse_args(int argc, char** argv) {
     else if (a == "--interp") o.interp = next() == "trilinear" ? EMC_INTERP_TRILINEAR : EMC_INTERP_NEAREST;
     else if (a == "--out") o.out = next();
     else if (a == "--iterations") o.iterations = std::atoi(next().c_str());
+    else if (a == "--graph") o.graph = true;
+    else if (a == "--prune") o.prune = true;
     else if (!a.empty() && a[0] != '-') o.conf = a;
     else die("unknown option", a.c_str());
   }
@@ -286,6 +296,8 @@ int main(int argc, char** argv) {
       rc = emc_plan_bind(plan, d_images, d_mask, d_x, d_y, d_z, d_rot, d_w);
     }
     check(rc, ctx, "plan_bind");
+    if (o.prune) check(emc_plan_set_pruning(plan, 1, 0.999f, 1.0f, 0), ctx, "plan_set_pruning");
+    if (o.graph) check(emc_plan_capture(plan, d_model, d_weight), ctx, "plan_capture");
   } else {
     check(emc_allocate_real(ctx, &d_resp, (size_t)R * N), ctx, "alloc");
     check(emc_allocate_real(ctx, &d_scal, (size_t)R * N), ctx, "alloc");
@@ -307,7 +319,12 @@ int main(int argc, char** argv) {
     double ll = 0.0, mean_before = 0.0;
     if (!o.dropin) {
       emc_iter_stats st;
-      check(emc_iterate(plan, d_model, d_weight, sigma, &st), ctx, "iterate");
+      if (o.graph) {
+        check(emc_plan_replay(plan, sigma), ctx, "plan_replay");
+        check(emc_plan_wait(plan, &st), ctx, "plan_wait");
+      } else {
+        check(emc_iterate(plan, d_model, d_weight, sigma, &st), ctx, "iterate");
+      }
       ll = st.total_loglik;
       mean_before = st.model_mean_before;
     } else {
@@ -389,6 +406,15 @@ int main(int argc, char** argv) {
       const float* src = d_resp;
       if (!o.dropin) emc_plan_results(plan, &src, nullptr, nullptr);
       check(emc_copy_real_to_host(ctx, h_resp.data(), src, R * N), ctx, "copy");
+      if (o.prune) {  // back to the input order of patterns and rotations
+        std::vector<int> po(N), ro(R);
+        emc_plan_pattern_order(plan, po.data());
+        emc_plan_rotation_order(plan, ro.data());
+        std::vector<float> t(h_resp.size());
+        for (int r = 0; r < R; ++r)
+          for (int i = 0; i < N; ++i) t[(size_t)ro[r] * N + po[i]] = h_resp[(size_t)r * N + i];
+        h_resp.swap(t);
+      }
       char name[64];
       std::snprintf(name, sizeof name, "/debug/respons_%04d.data", it);
       write_raw(o.out + name, h_resp.data(), h_resp.size());

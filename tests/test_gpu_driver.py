@@ -103,3 +103,30 @@ def test_driver_model_init_modes(prob, tmp_path, model_input, dropin):
     assert len(logs) == 1 and np.isfinite(logs[0]["total_loglik"])
     m = np.fromfile(tmp_path / "out" / "output" / "model_0000.bin", np.float32)
     assert np.all(np.isfinite(m)) and m.max() > 0
+
+
+def test_driver_graph_replay_matches_direct(prob, tmp_path):
+    """--graph replays one captured iteration: the same files as direct calls."""
+    conf = S.write_problem(prob, tmp_path / "in", iterations=2)
+    a = run_driver(conf, tmp_path / "a", "--deterministic")
+    b = run_driver(conf, tmp_path / "b", "--deterministic", "--graph")
+    assert [x["total_loglik"] for x in a] == [x["total_loglik"] for x in b]
+    for name in ("model_0001.bin", "weight_0001.bin"):
+        assert np.array_equal(np.fromfile(tmp_path / "a" / "output" / name, np.float32),
+                              np.fromfile(tmp_path / "b" / "output" / name, np.float32))
+
+
+def test_driver_prune_writes_input_order(prob, tmp_path):
+    """--prune keeps the plan's rotations and patterns in its own order; the
+    debug responsibilities come back in the input order (here every iteration
+    is a full scan: the first always is, and at sigma 0.4 this likelihood is
+    too broad to prune)."""
+    conf = S.write_problem(prob, tmp_path / "in", iterations=2)
+    a = run_driver(conf, tmp_path / "a", "--precision", "mixed", "--deterministic")
+    b = run_driver(conf, tmp_path / "b", "--precision", "mixed", "--deterministic", "--prune")
+    R, N = prob.quats.shape[0], prob.images.shape[0]
+    for it in range(2):
+        assert abs(a[it]["total_loglik"] - b[it]["total_loglik"]) <= 1e-5 * abs(a[it]["total_loglik"])
+        ra = np.fromfile(tmp_path / "a" / "debug" / f"respons_{it:04d}.data", np.float32)
+        rb = np.fromfile(tmp_path / "b" / "debug" / f"respons_{it:04d}.data", np.float32)
+        assert np.abs(ra.reshape(R, N) - rb.reshape(R, N)).max() < 1e-4

@@ -200,7 +200,9 @@ def workload_desc(prob, precision, insert):
             "side": c.side, "n_images": c.n_images, "n_rot": int(prob.quats.shape[0]),
             "p_eff": int(prob.mask.sum()), "interp": "nearest",
             "precision": precision, "insert": insert,
-            "l2": "inputs larger than L2 (patterns 1.3 GB, responsibilities 2 GB per step)"}
+            "l2": f"inputs larger than L2 (patterns {prob.images.nbytes / 1e9:.1f} GB, "
+                  f"responsibilities {4.0 * prob.quats.shape[0] * c.n_images / 1e9:.1f} GB "
+                  f"per step)"}
 
 
 # ---------------------------------------------------- CPU (oracle) leg ----
@@ -242,6 +244,7 @@ def run_ours(args):
     ws, rank, local = dist_setup(args)
     dev = torch.device(f"cuda:{local}")
     prob = make_problem(args.config, "cuda")
+    torch.cuda.empty_cache()  # the generator's buffers go back to the device for the plan
     s, R, N = prob.cfg.side, prob.quats.shape[0], prob.images.shape[0]
     ctx = E.Context(local)
     # one explicit stream for torch copies and library kernels (the legacy

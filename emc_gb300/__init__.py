@@ -15,6 +15,7 @@ context's last error text, where the reference printed and continued.
 """
 from __future__ import annotations
 
+import atexit
 import ctypes as C
 import weakref
 
@@ -111,6 +112,21 @@ def read_config(path=None, text=None) -> "_lib.Config":
     return cfg
 
 
+_LIVE_CONTEXTS = weakref.WeakSet()
+
+
+@atexit.register
+def _close_all():
+    """Destroy what is still open while the CUDA runtime is alive: at
+    interpreter exit objects are otherwise collected in no particular order,
+    after the runtime's own teardown may have begun."""
+    for ctx in list(_LIVE_CONTEXTS):
+        try:
+            ctx.close()
+        except Exception:
+            pass
+
+
 class Context:
     """One device, one stream (replaces cuda_set_device, emc_cuda.cu:867-870)."""
 
@@ -123,6 +139,7 @@ class Context:
         self._h = h
         self.device = device
         self._children = weakref.WeakSet()  # plans and batches, closed before the context
+        _LIVE_CONTEXTS.add(self)
 
     # -- plumbing ------------------------------------------------------------
     @property
@@ -376,6 +393,7 @@ class Plan:
     OPT_ESTEP_GHLO = 3
     OPT_MSTEP_QLO = 2
     OPT_MSTEP_AGGREGATE = 4
+    OPT_COUNTS_ROUND = 5
 
     def set_option(self, option: int, value: int):
         self.ctx._check(self._lib.emc_plan_set_option(self._h, option, value), "plan_set_option")

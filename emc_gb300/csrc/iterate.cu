@@ -88,15 +88,22 @@ __global__ void pattern_ops_kernel(const float* __restrict__ images, const int* 
                                    float* __restrict__ Kraw, float* __restrict__ Kt,
                                    float* __restrict__ K2, int* __restrict__ flags,
                                    const int* __restrict__ perm) {
-  const int i = blockIdx.y;
-  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.x;  // patterns on x: N may exceed the 65,535 of y
+  const int q = blockIdx.y * blockDim.x + threadIdx.x;
   if (q >= Kp) return;
   const int p = pix[q];
   float k = 0.0f;
   if (p >= 0) {
     const float v = __ldg(images + (size_t)(perm ? perm[i] : i) * n2 + p);
     if (!isfinite(v)) atomicOr(flags, 1);
-    if (!(v >= 0.0f && v <= 2048.0f && v == rintf(v))) atomicOr(flags, 2);
+    // bit 1: not an integer in [0, 65504] (no FP16 form); bit 3: an integer
+    // above 2048 (FP16 rounds it); flags[8]: the largest integer count
+    if (!(v >= 0.0f && v <= 65504.0f && v == rintf(v))) {
+      atomicOr(flags, 2);
+    } else {
+      if (v > 2048.0f) atomicOr(flags, 8);
+      atomicMax(flags + 8, (int)v);
+    }
     k = __fmul_rn(v, __ldg(cnorm + i));
   }
   const size_t o = (size_t)i * Kp + q;
@@ -981,7 +988,7 @@ int emc::pattern_side(emc_plan* p, const int* d_perm, bool with_tc) {
       p->images, p->mask, n2, N, p->d.normalize_images, p->cnorm, d_perm);
   if ((rc = after_launch(ctx, "pattern_norm_kernel"))) return rc;
   // Kt / K2 exist only for the FP32 path (null: not written).
-  pattern_ops_kernel<<<dim3(ceil_div(p->Kp, 256), N), 256, 0, ctx->stream>>>(
+  pattern_ops_kernel<<<dim3(N, ceil_div(p->Kp, 256)), 256, 0, ctx->stream>>>(
       p->images, p->pix, p->cnorm, n2, N, p->Kp, p->Kraw, p->Kt, p->K2, p->flags, d_perm);
   if ((rc = after_launch(ctx, "pattern_ops_kernel"))) return rc;
   row_sum_kernel<<<N, 256, 0, ctx->stream>>>(p->Kraw, p->Kp, p->Kp, p->Ksum);
@@ -1057,7 +1064,9 @@ extern "C" int emc_plan_bind(emc_plan* p, const float* d_images, const int* d_ma
   EMC_CUDA(ctx, cudaMemcpyAsync(hflags, p->flags, sizeof(hflags), cudaMemcpyDeviceToHost, ctx->stream));
   EMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   if (hflags[0] & 1) return fail(ctx, EMC_ERR_NONFINITE, "plan_bind: images contain NaN/Inf");
-  p->counts_fp16_exact = !(hflags[0] & 2);
+  p->counts_fp16_exact = !(hflags[0] & 2) && !(hflags[0] & 8);
+  p->counts_integer = !(hflags[0] & 2);
+  p->count_max = hflags[8];
   p->images = d_images;
   p->mask = d_mask;
   p->x = d_x;
@@ -1449,10 +1458,16 @@ extern "C" int emc_plan_set_option(emc_plan* p, int option, int value) {
     p->mstep_aggregate = value;
     return EMC_OK;
   }
+  if (option == EMC_OPT_COUNTS_ROUND) {
+    EMC_REQUIRE(ctx, value == 0 || value == 1, "plan_set_option: counts_round %d", value);
+    EMC_REQUIRE(ctx, !p->tc, "plan_set_option: set EMC_OPT_COUNTS_ROUND before bind");
+    p->counts_round = value;
+    return EMC_OK;
+  }
   if (option == EMC_OPT_MSTEP_QLO) {
     EMC_REQUIRE(ctx, value == 0 || value == 1, "plan_set_option: q_lo %d", value);
     p->mstep_q_lo = value;
-    return EMC_OK;
+    return value ? tc_ensure_qlo(p) : EMC_OK;
   }
   return fail(ctx, EMC_ERR_INVALID, "plan_set_option: unknown option %d", option);
 }

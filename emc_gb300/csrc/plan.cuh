@@ -22,6 +22,10 @@ struct emc_plan {
   int n_rt = 0;    // rotation tiles of EMC_RT
   bool bound = false;
   bool counts_fp16_exact = false;  // every count is an integer in [0, 2048]
+  bool counts_integer = false;     // every count is an integer in [0, 65504]
+  int count_max = 0;               // the largest count
+  int counts_round = 0;            // tensor path: counts above 2048 rounded to FP16
+  float k2_scale = 1.0f / 128.0f;  // K^2 operand = k^2 k2_scale (hi + lo), set at bind
 
   // bound inputs (caller owned)
   const float* images = nullptr;
@@ -122,6 +126,7 @@ int prune_iterate(emc_plan* p, float* model, float* weight, float sigma, emc_ite
 void prune_free(emc_plan* p);
 int prune_reset(emc_plan* p);
 int tc_pattern_side(emc_plan* p, const int* d_perm);
+int tc_ensure_qlo(emc_plan* p);
 int pattern_side(emc_plan* p, const int* d_perm, bool with_tc);
 int tc_estep(emc_plan* p);
 int tc_mstep(emc_plan* p, float* model, float* weight);

@@ -81,28 +81,33 @@ static int make_map(emc_ctx* ctx, CUtensorMap* map, const void* base, uint64_t r
 }
 
 // ---------------------------------------------------- pattern operands ---
-constexpr float kK2Scale = 1.0f / 128.0f;  // K^2 * 2^-7 <= 2^15 for counts <= 2048
+
 constexpr float kMSScale = 1.0f / 256.0f;  // (M' S) * 2^-8 keeps slices below 2^24 in range
 
 // Counts -> FP16 operands, rows of Kp (patterns padded to Np with zeros):
-// Kh = k, K2h + K2l = k^2 * 2^-7 exactly (K2h == nullptr: Kh only).
+// Kh = fp16(k) (k itself up to 2048; larger counts rounded to 11 significant
+// bits), K2h + K2l = Kh^2 * k2_scale exactly (Kh^2 has at most 22 significant
+// bits, and k2_scale keeps the largest below 2^15 and every value a multiple
+// of 2^-24) (K2h == nullptr: Kh only).
 __global__ void tc_pattern_ops_kernel(const float* __restrict__ images, const int* __restrict__ pix,
                                       int n2, int N, int Kp, __half* __restrict__ Kh,
                                       __half* __restrict__ K2h, __half* __restrict__ K2l,
-                                      const int* __restrict__ perm) {
-  const int i = blockIdx.y;
-  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+                                      const int* __restrict__ perm, float k2_scale) {
+  const int i = blockIdx.x;  // patterns on x: Np may exceed the 65,535 of y
+  const int q = blockIdx.y * blockDim.x + threadIdx.x;
   if (q >= Kp) return;
   float k = 0.0f;
   if (i < N) {
     const int p = pix[q];
     if (p >= 0) k = __ldg(images + (size_t)(perm ? perm[i] : i) * n2 + p);
   }
-  const float k2 = k * k * kK2Scale;  // exact: k^2 < 2^22
+  const __half kh = __float2half_rn(k);
+  const float kr = __half2float(kh);
+  const float k2 = kr * kr * k2_scale;  // exact in FP32: 22 significant bits
   const __half hi = __float2half_rn(k2);
   const __half lo = __float2half_rn(k2 - __half2float(hi));
   const size_t o = (size_t)i * Kp + q;
-  Kh[o] = __float2half_rn(k);
+  Kh[o] = kh;
   if (K2h) {
     K2h[o] = hi;
     K2l[o] = lo;
@@ -218,6 +223,7 @@ struct TcEstepArgs {
   const float* rot_A;
   const float* rotw;
   const float* cnorm;   // c_i (phi is stored as c_i num/den)
+  float k2_inv;         // 1 / k2_scale of the K^2 operand
   const float* sigma;   // [1] annealing width (device memory)
   int known_intensity;
   float* L;
@@ -364,8 +370,8 @@ __global__ void __launch_bounds__(es::THREADS, 1)
         for (int j = 0; j < 16; ++j) {
           const int cl = c0 + j;
           const int r = r0 + cl;
-          const float num = vn[j] * 128.0f, den = vd[j] * 256.0f;
-          const float B = vb[j], Cc = vc[j] * 128.0f;
+          const float num = vn[j] * a.k2_inv, den = vd[j] * 256.0f;
+          const float B = vb[j], Cc = vc[j] * a.k2_inv;
           const float sc = s_scale[cl];
           bool ok = nok && r < a.R && sc > 0.0f;
           float iphi = 1.0f, phi = 1.0f;
@@ -889,9 +895,17 @@ static TcState* state(emc_plan* p) { return (TcState*)p->tc; }
 
 int tc_bind(emc_plan* p) {
   emc_ctx* ctx = p->ctx;
-  if (!p->counts_fp16_exact)
+  if (!p->counts_integer || (!p->counts_fp16_exact && !p->counts_round))
     return fail(ctx, EMC_ERR_UNSUPPORTED,
-                "mixed precision needs integer counts in [0, 2048] (exact in FP16)");
+                "mixed precision needs integer counts in [0, 2048] (exact in FP16), or in [0, "
+                "65504] with EMC_OPT_COUNTS_ROUND (largest count here %d)", p->count_max);
+  {
+    // K^2 scale: the largest FP16 count squared times k2_scale stays below 2^15
+    const float km = __half2float(__float2half_rn((float)p->count_max));
+    int e = 7;
+    while (km * km * std::ldexp(1.0f, -e) > 32768.0f) ++e;
+    p->k2_scale = std::ldexp(1.0f, -e);
+  }
   if (p->d.diff != EMC_DIFF_POISSON && p->d.diff != EMC_DIFF_TRUE_POISSON)
     return fail(ctx, EMC_ERR_UNSUPPORTED,
                 "mixed precision implements the poisson and true-poisson likelihoods");
@@ -914,13 +928,11 @@ int tc_bind(emc_plan* p) {
     for (int j = 0; j < (pois ? 2 : 6); ++j)
       if (!rc) rc = plan_alloc(p, (void**)rot_ops[j], rk * 2);
     if (!rc) rc = plan_alloc(p, (void**)&p->Qh, (size_t)Rp * Np * 2);
-    if (!rc) rc = plan_alloc(p, (void**)&p->Ql, (size_t)Rp * Np * 2);
     if (!rc) rc = plan_alloc(p, (void**)&p->qscale, (size_t)Rp * 4);
     if (!rc) rc = plan_alloc(p, (void**)&st->status, 64);
     if (rc) return rc;
     EMC_CUDA(ctx, cudaMemsetAsync(st->status, 0, 64, ctx->stream));
     EMC_CUDA(ctx, cudaMemsetAsync(p->Qh, 0, (size_t)Rp * Np * 2, ctx->stream));
-    EMC_CUDA(ctx, cudaMemsetAsync(p->Ql, 0, (size_t)Rp * Np * 2, ctx->stream));
     // tensor maps (fixed addresses for the plan's lifetime)
     if (!rc) rc = make_map(ctx, &st->mK, p->Kh, Np, Kp, 128, 32);
     if (pois) {
@@ -933,7 +945,6 @@ int tc_bind(emc_plan* p) {
       for (int j = 0; j < 6 && !rc; ++j) rc = make_map(ctx, &st->rot[j], ro[j], Rp, Kp, 128, 32);
     }
     if (!rc) rc = make_map(ctx, &st->mQh, p->Qh, Rp, Np, 128, 64);
-    if (!rc) rc = make_map(ctx, &st->mQl, p->Ql, Rp, Np, 128, 64);
     if (!rc) rc = make_map(ctx, &st->mKt, p->KhT, Kp, Np, 256, 64);
     if (rc) return rc;
     EMC_CUDA(ctx, cudaFuncSetAttribute(tc_estep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -943,6 +954,7 @@ int tc_bind(emc_plan* p) {
     EMC_CUDA(ctx, cudaFuncSetAttribute(tc_mstep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        ms::SMEM_BYTES));
   }
+  if (p->mstep_q_lo && (rc = tc_ensure_qlo(p))) return rc;
   return tc_pattern_side(p, nullptr);
 }
 
@@ -953,8 +965,9 @@ int tc_pattern_side(emc_plan* p, const int* d_perm) {
   const int N = p->d.n_images, Np = p->Np, Kp = p->Kp;
   const bool pois = p->d.diff == EMC_DIFF_TRUE_POISSON;
   int rc;
-  tc_pattern_ops_kernel<<<dim3(ceil_div(Kp, 256), Np), 256, 0, ctx->stream>>>(
-      p->images, p->pix, p->n2, N, Kp, p->Kh, pois ? nullptr : p->K2hi, p->K2lo, d_perm);
+  tc_pattern_ops_kernel<<<dim3(Np, ceil_div(Kp, 256)), 256, 0, ctx->stream>>>(
+      p->images, p->pix, p->n2, N, Kp, p->Kh, pois ? nullptr : p->K2hi, p->K2lo, d_perm,
+      p->k2_scale);
   if ((rc = after_launch(ctx, "tc_pattern_ops_kernel"))) return rc;
   if (!pois) tc_k2lo_flags_kernel<<<dim3(Kp / 32, Np / 128), 256, 0, ctx->stream>>>(p->K2lo, Kp, p->k2lo_any,
                                                                          Kp / 32);
@@ -965,6 +978,18 @@ int tc_pattern_side(emc_plan* p, const int* d_perm) {
 }
 
 int* tc_status(emc_plan* p) { return p->tc ? state(p)->status : nullptr; }
+
+// The FP16 lo half of the M-step operand and its tensor map, allocated the
+// first time an M-step that uses it is requested (it is never read otherwise).
+int tc_ensure_qlo(emc_plan* p) {
+  if (!p->tc || p->Ql) return EMC_OK;
+  emc_ctx* ctx = p->ctx;
+  const size_t bytes = (size_t)p->Rp * p->Np * 2;
+  int rc = plan_alloc(p, (void**)&p->Ql, bytes);
+  if (rc) return rc;
+  EMC_CUDA(ctx, cudaMemsetAsync(p->Ql, 0, bytes, ctx->stream));
+  return make_map(ctx, &state(p)->mQl, p->Ql, p->Rp, p->Np, 128, 64);
+}
 
 static int tc_estep_pois(emc_plan* p) {
   emc_ctx* ctx = p->ctx;
@@ -1018,6 +1043,7 @@ int tc_estep(emc_plan* p) {
   a.gh_lo = p->estep_gh_lo >= 0 ? p->estep_gh_lo : (p->d.known_intensity ? 3 : 1);
   a.tiles = p->prune_tiles;
   a.k2lo_any = p->k2lo_any;
+  a.k2_inv = 1.0f / p->k2_scale;
   a.rot_cnt = p->rot_cnt;
   a.rot_A = p->rot_A;
   a.rotw = p->rotw;

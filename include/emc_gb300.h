@@ -386,6 +386,12 @@ int emc_batch_destroy(emc_batch* batch);
  * insertions that land on the same voxel before one atomic (float atomics
  * only); 0 (default) issues one atomic per rotation-pixel pair. */
 #define EMC_OPT_MSTEP_AGGREGATE 4
+/* EMC_OPT_COUNTS_ROUND: the tensor-core path takes counts as FP16, exact for
+ * integers up to 2048.  0 (default): bind rejects larger counts
+ * (EMC_ERR_UNSUPPORTED); 1: integer counts up to 65504 are accepted and those
+ * above 2048 are rounded to the nearest FP16 value (relative error <= 2^-12,
+ * only at those pixels).  Set before emc_plan_bind. */
+#define EMC_OPT_COUNTS_ROUND 5
 int emc_plan_set_option(emc_plan* plan, int option, int value);
 /* Instrumentation: with profiling on, emc_iterate records CUDA events on the
  * context stream between its phases; emc_plan_phase_ms (after the iteration

@@ -265,3 +265,42 @@ def test_lowcount_matches_oracle_and_reruns_bit_identical(ctx, cuda, lowcount, p
     b = run_plan(ctx, lowcount, cuda, precision=precision, insert_mode=E.INSERT_DETERMINISTIC)
     assert np.array_equal(a["model"], b["model"]) and np.array_equal(a["weight"], b["weight"])
     assert np.array_equal(a["respons"], b["respons"])
+
+
+def test_qlo_switched_on_after_bind(ctx, cuda, prob):
+    """The FP16 lo half of the M-step operand exists only once asked for; asking
+    after bind allocates it and the iteration uses it."""
+    s, R, N = prob.cfg.side, prob.quats.shape[0], prob.images.shape[0]
+    plan = E.Plan(ctx, s, N, R, precision=E.PREC_MIXED, insert_mode=E.INSERT_DETERMINISTIC)
+    plan.bind(T(prob.images, cuda), T(prob.mask, cuda, torch.int32), T(prob.x, cuda),
+              T(prob.y, cuda), T(prob.z, cuda), T(prob.quats, cuda), T(prob.weights, cuda))
+    before = plan.workspace_bytes
+    plan.set_option(E.Plan.OPT_MSTEP_QLO, 1)
+    assert plan.workspace_bytes > before
+    m = T(prob.init_model, cuda)
+    w = torch.empty_like(m)
+    plan.iterate(m, w, 0.3)
+    ref = run_plan(ctx, prob, cuda, precision=E.PREC_MIXED, insert_mode=E.INSERT_DETERMINISTIC,
+                   options={E.Plan.OPT_MSTEP_QLO: 1})
+    assert np.array_equal(m.cpu().numpy().astype(np.float64), ref["model"])
+    plan.close()
+
+
+def test_counts_above_2048_rounded_to_fp16(ctx, cuda, prob):
+    """Bright patterns: counts up to ~30,000.  Without EMC_OPT_COUNTS_ROUND the
+    tensor path refuses them; with it, it matches the FP64 oracle run on the
+    counts rounded to FP16 (the K^2 operand scale follows the largest count)."""
+    p = S.Problem(**{**prob.__dict__})
+    p.images = (prob.images * 37.0).astype(np.float32)
+    assert p.images.max() > 4096
+    with pytest.raises(E.EmcError, match="UNSUPPORTED"):
+        run_plan(ctx, p, cuda, precision=E.PREC_MIXED)
+    got = run_plan(ctx, p, cuda, precision=E.PREC_MIXED, options={E.Plan.OPT_COUNTS_ROUND: 1})
+    rounded = p.images.astype(np.float16).astype(np.float32)
+    s = p.cfg.side
+    want = O.fused_iteration_fp64(p.init_model, rounded, p.mask, p.x, p.y, p.z, p.quats,
+                                  p.weights, 0.3, s)
+    tl, tphi, tm, tr = TOL[E.PREC_MIXED]
+    assert abs(got["stats"].total_loglik - want["total_loglik"]) <= tl * abs(want["total_loglik"])
+    np.testing.assert_allclose(got["phi"], want["phi"], rtol=tphi)
+    assert rel_l2(got["model"], want["model"]) < 2 * tm

@@ -59,6 +59,14 @@ def parse():
     ap.add_argument("--estep-ghlo", type=int, choices=[-1, 0, 1, 2, 3], default=-1,
                     help="tensor E-step: lo terms of G (bit 0) and H (bit 1); -1: the library's "
                          "default (G, and H when the intensity is known)")
+    ap.add_argument("--counts-round", type=int, choices=[-1, 0, 1], default=-1,
+                    help="tensor path: round counts above 2,048 to the nearest FP16 value "
+                         "(relative change <= 2^-12 on those pixels); without it such "
+                         "patterns run on the FP32 path.  -1: on for the large configuration "
+                         "(FP16 counts by its definition), off otherwise")
+    ap.add_argument("--raster", type=int, default=0,
+                    help="tensor path: the likelihood kernel's tile order (EMC_OPT_ESTEP_RASTER); "
+                         "0 (default): chosen by emc_plan_autotune before the warm-up")
     ap.add_argument("--plain-steps", type=int, default=2)
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
@@ -68,7 +76,10 @@ def parse():
                          "CUDA kernels (0: skip them)")
     ap.add_argument("--prune-steps", type=int, default=4,
                     help="timed iterations of the pruned-vs-full leg (0: skip)")
-    return ap.parse_args()
+    args = ap.parse_args()
+    if args.counts_round < 0:
+        args.counts_round = int(args.config == "large")
+    return args
 
 
 # ------------------------------------------------------------ helpers ----
@@ -263,6 +274,8 @@ def run_ours(args):
         p.set_option(E.Plan.OPT_MSTEP_QLO, args.mstep_qlo)
         p.set_option(E.Plan.OPT_ESTEP_GHLO, args.estep_ghlo)
         p.set_option(E.Plan.OPT_MSTEP_AGGREGATE, args.mstep_aggregate)
+        if prec == E.PREC_MIXED and args.counts_round:
+            p.set_option(E.Plan.OPT_COUNTS_ROUND, 1)
         p.bind(images, mask, x, y, z, rot, w)
         return p
 
@@ -283,6 +296,16 @@ def run_ours(args):
     model = T(prob.init_model)
     weight = torch.empty_like(model)
     sig = [E.sigma_schedule(i, 0.4, 0.12, 25) for i in range(args.warmup + args.steps)]
+    tuning = None
+    if precision == "mixed":
+        if args.raster:
+            plan.set_option(E.Plan.OPT_ESTEP_RASTER, args.raster)
+            tuning = {"estep_raster": args.raster, "source": "--raster"}
+        else:
+            t0 = time.perf_counter()
+            r, ms = plan.autotune(model, sig[0])
+            tuning = {"estep_raster": r, "source": "emc_plan_autotune",
+                      "prefix_ms": ms, "tuning_s": time.perf_counter() - t0}
     for i in range(args.warmup):
         plan.iterate(model, weight, sig[i], stats=False)
     torch.cuda.synchronize()
@@ -341,10 +364,13 @@ def run_ours(args):
         e2e = run_e2e(args, prob, plan, images, mask, x, y, z, rot, w, model, weight, sig,
                       torch_stream, ws, pairs)
     pruned = None
+    workspace = plan.workspace_bytes
     if precision == "mixed" and args.prune_steps > 0 and rank == 0:
+        plan.close()  # the prune leg's plans need the device memory
+        torch.cuda.synchronize()
         pruned = prune_leg(args, prob, ctx, T, (images, mask, x, y, z, rot, w), pairs)
-    return finish(args, prob, plan, ctx, ws, rank, precision, value, ms_step, st, plain, e2e,
-                  estep_ms, phases, launches, clocks, pairs, pruned)
+    return finish(args, prob, workspace, ctx, ws, rank, precision, value, ms_step, st, plain, e2e,
+                  estep_ms, phases, launches, clocks, pairs, pruned, tuning)
 
 
 def prune_leg(args, prob, ctx, T, inputs, pairs):
@@ -361,19 +387,25 @@ def prune_leg(args, prob, ctx, T, inputs, pairs):
     import emc_gb300 as E
     s, R, N = prob.cfg.side, prob.quats.shape[0], prob.images.shape[0]
 
-    def plan_b():
+    def plan_b(raster=0):
         p = E.Plan(ctx, s, N, R, diff=E.DIFF_TRUE_POISSON, precision=E.PREC_MIXED)
+        if args.counts_round:
+            p.set_option(E.Plan.OPT_COUNTS_ROUND, 1)
         p.bind(*inputs)
+        if raster:
+            p.set_option(E.Plan.OPT_ESTEP_RASTER, raster)
         return p
-    full = plan_b()
+    full = plan_b(args.raster)
     m0 = T(prob.true_model)
     ctx.normalize_model(s, m0)
+    raster = args.raster or full.autotune(m0, 0.12)[0]
     w0 = torch.empty_like(m0)
     for _ in range(3):
         full.iterate(m0, w0, 0.12, stats=False)
     runs = {}
     for kind in ("full", "pruned"):
-        plan = full if kind == "full" else plan_b()
+        # one plan at a time: at 256^3 a plan takes most of the device memory
+        plan = full if kind == "full" else plan_b(raster)
         if kind == "pruned":
             plan.set_pruning(True, min_mass=0.999, dilate=1.0)
         m = m0.clone()
@@ -388,9 +420,8 @@ def prune_leg(args, prob, ctx, T, inputs, pairs):
             t.append(time.perf_counter() - t0)
         runs[kind] = (statistics.mean(t), m.cpu().numpy().astype(np.float64),
                       plan.prune_info() if kind == "pruned" else None)
-        if kind == "pruned":
-            plan.close()
-    full.close()
+        plan.close()
+        torch.cuda.synchronize()
     tf, mf, _ = runs["full"]
     tp, mp, info = runs["pruned"]
     return {"likelihood": "true poisson (counts x log slice), mixed precision",
@@ -403,7 +434,7 @@ def prune_leg(args, prob, ctx, T, inputs, pairs):
             "active_fraction": info["active_fraction"], "core_fraction": info["core_fraction"],
             "pruned_iterations": info["pruned_iterations"],
             "fallback_iterations": info["fallback_iterations"],
-            "full_iterations": info["full_iterations"],
+            "full_iterations": info["full_iterations"], "estep_raster": raster,
             "model_rel_l2_vs_full_scan": float(np.linalg.norm(mp - mf) / np.linalg.norm(mf))}
 
 
@@ -438,8 +469,8 @@ def run_e2e(args, prob, plan, images, mask, x, y, z, rot, w, model, weight, sig,
             "ms_per_step": e2e_ms}
 
 
-def finish(args, prob, plan, ctx, ws, rank, precision, value, ms_step, st, plain, e2e, estep_ms,
-           phases, launches, clocks, pairs, pruned=None):
+def finish(args, prob, workspace, ctx, ws, rank, precision, value, ms_step, st, plain, e2e,
+           estep_ms, phases, launches, clocks, pairs, pruned=None, tuning=None):
     # ---- roofline of the dominant kernel (E-step)
     peaks = load_peaks()
     p_eff = int(prob.mask.sum())
@@ -472,7 +503,7 @@ def finish(args, prob, plan, ctx, ws, rank, precision, value, ms_step, st, plain
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32" if precision == "fp32" else "f16/f32",
-            "data": "synthetic (seeded; shapes of the mid-size configuration)",
+            "data": f"synthetic (seeded; shapes of the {args.config} configuration)",
             "config": dict(workload_desc(prob, precision, args.insert),
                            diff="poisson (reference)" if args.diff == "poisson"
                            else "true poisson (counts x log slice)",
@@ -480,14 +511,16 @@ def finish(args, prob, plan, ctx, ws, rank, precision, value, ms_step, st, plain
                            estep_gh={-1: "G fp16 hi+lo, H fp16 hi", 3: "G, H fp16 hi+lo",
                                      2: "G hi, H hi+lo", 1: "G hi+lo, H hi",
                                      0: "G, H fp16 hi"}[args.estep_ghlo],
-                           mstep_atomics="warp-aggregated" if args.mstep_aggregate else "per pair"),
+                           mstep_atomics="warp-aggregated" if args.mstep_aggregate else "per pair",
+                           counts="counts above 2048 rounded to fp16" if
+                           (args.counts_round and precision == "mixed") else "exact"),
             "iter_per_s": ws * 1e3 / ms_step,
             "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "plain_fp32": plain,
             "pruned": pruned,
             "speedup_vs_plain_fp32": (plain["ms_per_step"] / ms_step) if plain else None,
             "phase_ms": phase_mean, "gpu_launches": launches, "clocks": clocks,
             "total_loglik": st.total_loglik, "captured_mass": st.captured_mass,
-            "workspace_gb": plan.workspace_bytes / 1e9,
+            "workspace_gb": workspace / 1e9, "tile_order": tuning,
         }
         print(json.dumps(line), flush=True)
     if ws > 1:
@@ -521,7 +554,7 @@ def run_reference(args):
     line = {"metric": METRIC, "impl": "reference", "value": v, "unit": UNIT, "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": R * N / v * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32/f64",
-            "data": "synthetic (seeded; shapes of the mid-size configuration)",
+            "data": f"synthetic (seeded; shapes of the {args.config} configuration)",
             "config": workload_desc(prob, "reference (quirk-exact CPU restatement)", "sequential"),
             "cpu_baseline": {**info, "value": v},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -633,7 +666,7 @@ def run_batched(args):
     from emc_gb300 import synthetic as S
     dev = torch.device("cuda:0")
     T = lambda a, dt=torch.float32: torch.as_tensor(np.ascontiguousarray(a), dtype=dt, device=dev)
-    ctxs, plans, models, weights, keep, pairs = [], [], [], [], [], []
+    ctxs, plans, models, weights, keep, pairs, rasters = [], [], [], [], [], [], []
     for k, (side, n, lvl) in enumerate(BATCHED):
         f = side / 64.0
         cfg = S.Config(f"batched{k}", side, 400, 1.5, 12 * f, n, 1000, (0.5, 1.5), 4 * f, lvl, 1,
@@ -647,6 +680,8 @@ def run_batched(args):
         plan.bind(*inputs)
         m = T(prob.init_model)
         c.normalize_model(side, m)
+        rasters.append(plan.autotune(m, 0.4)[0] if not args.raster else args.raster)
+        plan.set_option(E.Plan.OPT_ESTEP_RASTER, rasters[-1])
         w = torch.empty_like(m)
         ctxs.append(c)
         plans.append(plan)
@@ -683,8 +718,9 @@ def run_batched(args):
             "data": "synthetic (seeded; eight uneven problems)",
             "config": {"workload": "batched: 8 reconstructions 48^3..160^3, 500..30,000 "
                                    "patterns, rotation levels 3..8, one iteration each",
-                       "problems": [{"side": s, "n_images": n, "rot_n": l, "pairs": p}
-                                    for (s, n, l), p in zip(BATCHED, pairs)],
+                       "problems": [{"side": s, "n_images": n, "rot_n": l, "pairs": p,
+                                     "estep_raster": r}
+                                    for (s, n, l), p, r in zip(BATCHED, pairs, rasters)],
                        "total_pairs": total, "precision": "mixed",
                        "timing": "host clock around graph launches + synchronise"},
             "sequential": {"ms_per_step": t_seq * 1e3, "pairs_per_s": total / t_seq},

@@ -394,9 +394,33 @@ class Plan:
     OPT_MSTEP_QLO = 2
     OPT_MSTEP_AGGREGATE = 4
     OPT_COUNTS_ROUND = 5
+    OPT_ESTEP_RASTER = 6
 
     def set_option(self, option: int, value: int):
         self.ctx._check(self._lib.emc_plan_set_option(self._h, option, value), "plan_set_option")
+
+    def autotune(self, model, sigma: float = 0.4) -> tuple:
+        """Picks the likelihood kernel's tile order (OPT_ESTEP_RASTER) by
+        timing the candidates on `model` (emc_plan_autotune).  Returns
+        (raster, ms of the timed prefix); (0, 0.0) for FP32 plans."""
+        import ctypes as C
+        r, ms = C.c_int(0), C.c_float(0.0)
+        self.ctx._check(self._lib.emc_plan_autotune(self._h, _ptr(model, name="model"),
+                                                    float(sigma), C.byref(r), C.byref(ms)),
+                        "plan_autotune")
+        return r.value, ms.value
+
+    def time_likelihood(self, raster: int, first: int = 0, count: int = 1 << 30,
+                        model=None, sigma: float = 0.4) -> tuple:
+        """One timed launch of the likelihood kernel over tiles [first,
+        first + count) of order `raster` (emc_plan_time_likelihood); model
+        given: expanded first.  Returns (ms, tiles in the full grid)."""
+        import ctypes as C
+        ms, tot = C.c_float(0.0), C.c_int(0)
+        self.ctx._check(self._lib.emc_plan_time_likelihood(
+            self._h, _ptr(model, name="model"), float(sigma), int(raster), int(first),
+            int(count), C.byref(ms), C.byref(tot)), "plan_time_likelihood")
+        return ms.value, tot.value
 
     def set_profiling(self, on: bool = True):
         self.ctx._check(self._lib.emc_plan_set_profiling(self._h, int(on)), "plan_set_profiling")

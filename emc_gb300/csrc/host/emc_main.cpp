@@ -4,12 +4,14 @@
 //
 //   emc [config] [--dropin] [--precision fp32|mixed] [--deterministic]
 //       [--interp nearest|trilinear] [--out DIR] [--iterations N] [--graph]
-//       [--prune]
+//       [--prune] [--no-autotune]
 //
 // --graph records the fused iteration once as a CUDA graph and replays it
 // (emc_plan_capture / emc_plan_replay); --prune turns on pruned iterations
 // (emc_plan_set_pruning, mixed precision), whose debug responsibilities are
-// written back in the input pattern and rotation order.
+// written back in the input pattern and rotation order.  Mixed-precision
+// plans pick the likelihood kernel's tile order with emc_plan_autotune on the
+// start model unless --no-autotune is given (the results do not depend on it).
 //
 // config defaults to ../emc.conf as in main.cpp:66-70.  Inputs replace the
 // reference's HDF5 reads (emc_helper.cpp:198-368, absent libraries) by raw
@@ -61,6 +63,7 @@ struct Opts {
   int iterations = -1;
   bool graph = false;
   bool prune = false;
+  bool autotune = true;
 };
 
 [[noreturn]] void die(const char* what, const char* detail = "") {
@@ -134,6 +137,7 @@ Opts parse_args(int argc, char** argv) {
     else if (a == "--iterations") o.iterations = std::atoi(next().c_str());
     else if (a == "--graph") o.graph = true;
     else if (a == "--prune") o.prune = true;
+    else if (a == "--no-autotune") o.autotune = false;
     else if (!a.empty() && a[0] != '-') o.conf = a;
     else die("unknown option", a.c_str());
   }
@@ -296,6 +300,15 @@ int main(int argc, char** argv) {
       rc = emc_plan_bind(plan, d_images, d_mask, d_x, d_y, d_z, d_rot, d_w);
     }
     check(rc, ctx, "plan_bind");
+    if (o.autotune && d.precision == EMC_PREC_MIXED) {
+      int raster = 0;
+      float ms = 0.0f;
+      check(emc_plan_autotune(plan, d_model, emc_sigma_schedule(0, cfg.sigma_start, cfg.sigma_final,
+                                                                 cfg.sigma_half_life),
+                              &raster, &ms), ctx, "plan_autotune");
+      std::fprintf(stderr, "emc: likelihood tile order %d (%.3f ms on the timed prefix)\n", raster,
+                   ms);
+    }
     if (o.prune) check(emc_plan_set_pruning(plan, 1, 0.999f, 1.0f, 0), ctx, "plan_set_pruning");
     if (o.graph) check(emc_plan_capture(plan, d_model, d_weight), ctx, "plan_capture");
   } else {

@@ -1453,6 +1453,12 @@ extern "C" int emc_plan_set_option(emc_plan* p, int option, int value) {
     p->estep_gh_lo = value;
     return EMC_OK;
   }
+  if (option == EMC_OPT_ESTEP_RASTER) {
+    EMC_REQUIRE(ctx, value != 0 && value >= -4096 && value <= 4096,
+                "plan_set_option: raster %d", value);
+    p->estep_raster = value;
+    return EMC_OK;
+  }
   if (option == EMC_OPT_MSTEP_AGGREGATE) {
     EMC_REQUIRE(ctx, value == 0 || value == 1, "plan_set_option: aggregate %d", value);
     p->mstep_aggregate = value;
@@ -1470,6 +1476,47 @@ extern "C" int emc_plan_set_option(emc_plan* p, int option, int value) {
     return value ? tc_ensure_qlo(p) : EMC_OK;
   }
   return fail(ctx, EMC_ERR_INVALID, "plan_set_option: unknown option %d", option);
+}
+
+extern "C" int emc_plan_autotune(emc_plan* p, const float* d_model, float sigma, int* h_raster,
+                                 float* h_ms) {
+  if (!p) return EMC_ERR_INVALID;
+  emc_ctx* ctx = p->ctx;
+  EMC_REQUIRE(ctx, p->bound, "autotune: plan not bound");
+  EMC_REQUIRE(ctx, d_model, "autotune: null model");
+  if (p->d.precision != EMC_PREC_MIXED) {  // the FP32 path has no tile order to tune
+    if (h_raster) *h_raster = 0;
+    if (h_ms) *h_ms = 0.0f;
+    return EMC_OK;
+  }
+  int rc = set_sigma(p, sigma);
+  if (!rc) rc = plan_expand(p, d_model);
+  if (!rc) rc = tc_autotune(p, 256, h_raster, h_ms);
+  // the timed launches count non-finite pairs of partial grids: not an iteration's
+  if (!rc) EMC_CUDA(ctx, cudaMemsetAsync(p->flags + 4, 0, sizeof(int), ctx->stream));
+  if (!rc) EMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return rc;
+}
+
+extern "C" int emc_plan_time_likelihood(emc_plan* p, const float* d_model, float sigma,
+                                        int raster, int first_tile, int n_tiles, float* h_ms,
+                                        int* h_total_tiles) {
+  if (!p) return EMC_ERR_INVALID;
+  emc_ctx* ctx = p->ctx;
+  EMC_REQUIRE(ctx, p->bound, "time_likelihood: plan not bound");
+  EMC_REQUIRE(ctx, p->d.precision == EMC_PREC_MIXED, "time_likelihood: tensor-core plans only");
+  EMC_REQUIRE(ctx, raster != 0 && raster >= -4096 && raster <= 4096 && first_tile >= 0 &&
+                       n_tiles > 0 && h_ms, "time_likelihood: bad arguments");
+  int rc = EMC_OK;
+  if (d_model) {
+    rc = set_sigma(p, sigma);
+    if (!rc) rc = plan_expand(p, d_model);
+    if (!rc) rc = tc_estep_prepare(p);
+  }
+  if (!rc) rc = tc_time_estep(p, raster, first_tile, n_tiles, h_ms);
+  if (!rc && h_total_tiles) *h_total_tiles = tc_estep_tiles(p);
+  if (!rc) EMC_CUDA(ctx, cudaMemsetAsync(p->flags + 4, 0, sizeof(int), ctx->stream));
+  return rc;
 }
 
 extern "C" int emc_plan_set_profiling(emc_plan* p, int on) {

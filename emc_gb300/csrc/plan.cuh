@@ -98,6 +98,7 @@ struct emc_plan {
   void* tc = nullptr;  // tensor-core state (tensor maps, rotation operands)
   int estep_gh_lo = -1;   // tensor E-step lo terms: bit 0 G, bit 1 H; -1 auto
   int mstep_q_lo = 0;     // tensor M-step: Q as FP16 hi + lo (1) or hi only (0)
+  int estep_raster = 8;     // tensor E-step tile order (EMC_OPT_ESTEP_RASTER)
   int mstep_aggregate = 0;  // tensor M-step: warp-aggregated float atomics (nearest)
 
   std::vector<void*> allocs;
@@ -129,6 +130,10 @@ int tc_pattern_side(emc_plan* p, const int* d_perm);
 int tc_ensure_qlo(emc_plan* p);
 int pattern_side(emc_plan* p, const int* d_perm, bool with_tc);
 int tc_estep(emc_plan* p);
+int tc_autotune(emc_plan* p, int waves, int* best, float* best_ms);
+int tc_estep_prepare(emc_plan* p);  // rotation operands of the likelihood from the slices
+int tc_estep_tiles(emc_plan* p);    // tiles of the full likelihood grid
+int tc_time_estep(emc_plan* p, int raster, int first, int count, float* ms);
 int tc_mstep(emc_plan* p, float* model, float* weight);
 int* tc_status(emc_plan* p);  // device status word of the tensor-core pipelines
 void tc_free(emc_plan* p);

@@ -30,6 +30,8 @@
 #include <cuda.h>
 #include <cuda_fp16.h>
 
+#include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -211,11 +213,37 @@ constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 8192 + 1024;  // barriers, row
 constexpr int EPI_WARPS = 16;  // four per TMEM lane quarter, 32 columns each
 constexpr int EPI_PARTS = EPI_WARPS / 4;
 constexpr int THREADS = 64 + 32 * EPI_WARPS;
-constexpr int GROUP = 8;       // rotation tiles per raster group
 }  // namespace es
+
+// Tile of CTA b in a grouped raster over n_pt pattern tiles x n_rt rotation
+// tiles.  raster > 0: groups of `raster` rotation tiles, each group visiting
+// the pattern tiles in turn (the group's rotation panels are read by
+// consecutive CTAs); raster < 0: groups of -raster pattern tiles visiting the
+// rotation tiles in turn.
+__device__ __forceinline__ void raster_tile(int b, int raster, int n_pt, int n_rt, int& pt,
+                                            int& rt) {
+  if (raster > 0) {
+    const int per_group = raster * n_pt;
+    const int g = b / per_group, within = b % per_group;
+    const int rt0 = g * raster;
+    const int gsz = min(raster, n_rt - rt0);
+    rt = rt0 + within % gsz;
+    pt = within / gsz;
+  } else {
+    const int G = -raster;
+    const int per_group = G * n_rt;
+    const int g = b / per_group, within = b % per_group;
+    const int pt0 = g * G;
+    const int gsz = min(G, n_pt - pt0);
+    pt = pt0 + within % gsz;
+    rt = within / gsz;
+  }
+}
 
 struct TcEstepArgs {
   int N, R, Kp, n_pt, n_rt, nkb;
+  int raster;                     // tile order (raster_tile)
+  int tile0;                      // CTA b runs tile tile0 + b of the order
   int gh_lo;                      // lo terms: bit 0 G, bit 1 H (3: both, 0: hi only)
   const int2* tiles;              // pruned iteration: (pattern tile, rotation tile) per CTA
   const unsigned char* k2lo_any;  // [n_pt][nkb]
@@ -259,13 +287,8 @@ __global__ void __launch_bounds__(es::THREADS, 1)
     const int2 t = a.tiles[blockIdx.x];
     pt = t.x;
     rt = t.y;
-  } else {  // grouped raster: GROUP rotation tiles share each pattern tile in turn
-    const int per_group = GROUP * a.n_pt;
-    const int g = blockIdx.x / per_group, within = blockIdx.x % per_group;
-    const int rt0 = g * GROUP;
-    const int gsz = min(GROUP, a.n_rt - rt0);
-    rt = rt0 + within % gsz;
-    pt = within / gsz;
+  } else {
+    raster_tile(blockIdx.x + a.tile0, a.raster, a.n_pt, a.n_rt, pt, rt);
   }
   const int n0 = pt * BM, r0 = rt * BN;
 
@@ -440,11 +463,12 @@ constexpr int STAGE_BYTES = A_BYTES + 2 * B_BYTES;
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 256 + 2 * BN * 4 + 1024;
 constexpr int EPI_WARPS = 8;  // two per TMEM lane quarter, one per 128-column half
 constexpr int THREADS = 64 + 32 * EPI_WARPS;
-constexpr int GROUP = 8;
 }  // namespace ep
 
 struct TcEstepPoisArgs {
   int N, R, n_pt, n_rt, nkb;
+  int raster;             // tile order (raster_tile)
+  int tile0;              // CTA b runs tile tile0 + b of the order
   const int2* tiles;      // pruned iteration: (pattern tile, 256-rotation tile) per CTA
   int n_part;             // 128-rotation partial tiles
   const float* rot_ssum;  // S_r
@@ -479,12 +503,7 @@ __global__ void __launch_bounds__(ep::THREADS, 1)
     pt = t.x;
     rt = t.y;
   } else {
-    const int per_group = GROUP * a.n_pt;
-    const int g = blockIdx.x / per_group, within = blockIdx.x % per_group;
-    const int rt0 = g * GROUP;
-    const int gsz = min(GROUP, a.n_rt - rt0);
-    rt = rt0 + within % gsz;
-    pt = within / gsz;
+    raster_tile(blockIdx.x + a.tile0, a.raster, a.n_pt, a.n_rt, pt, rt);
   }
   const int n0 = pt * BM, r0 = rt * BN;
 
@@ -991,20 +1010,20 @@ int tc_ensure_qlo(emc_plan* p) {
   return make_map(ctx, &state(p)->mQl, p->Ql, p->Rp, p->Np, 128, 64);
 }
 
-static int tc_estep_pois(emc_plan* p) {
+// The likelihood kernels over tiles [first, first + count) of the full
+// (pattern tile, rotation tile) grid in the order `raster`, or over the plan's
+// pruned tile list (full == false and a list exists; first/count ignored).
+static int estep_pois_launch(emc_plan* p, int raster, int first, int count, bool full) {
   emc_ctx* ctx = p->ctx;
   TcState* st = state(p);
-  const size_t rk = (size_t)p->Rp * p->Kp;
-  int rc;
-  tc_rot_logs_kernel<<<ctx->sm_count * 8, 256, 0, ctx->stream>>>(p->S, rk, st->Gh, st->Gl);
-  if ((rc = after_launch(ctx, "tc_rot_logs_kernel"))) return rc;
   TcEstepPoisArgs a;
   a.N = p->d.n_images;
   a.R = p->d.n_rot;
   a.n_pt = p->Np / ep::BM;
   a.n_rt = ceil_div(p->Rp, ep::BN);
   a.nkb = p->Kp / ep::BK;
-  a.tiles = p->prune_tiles;
+  a.raster = raster;
+  a.tiles = full ? nullptr : p->prune_tiles;
   a.n_part = p->n_rt;
   a.rot_ssum = p->rot_ssum;
   a.rotw = p->rotw;
@@ -1015,22 +1034,34 @@ static int tc_estep_pois(emc_plan* p) {
   a.PHI = p->PHI;
   a.part = p->part;
   a.status = st->status;
-  const int grid = p->prune_tiles ? p->prune_n_tiles : a.n_pt * a.n_rt;
+  const int total = a.n_pt * a.n_rt;
+  first = a.tiles ? 0 : std::max(0, std::min(first, total));
+  const int grid = a.tiles ? p->prune_n_tiles : std::min(total - first, count);
+  a.tile0 = first;
   if (grid == 0) return EMC_OK;
   tc_estep_pois_kernel<<<grid, ep::THREADS, ep::SMEM_BYTES, ctx->stream>>>(st->mK, st->mLh,
                                                                            st->mLl, a);
   return after_launch(ctx, "tc_estep_pois_kernel");
 }
 
-int tc_estep(emc_plan* p) {
-  if (p->d.diff == EMC_DIFF_TRUE_POISSON) return tc_estep_pois(p);
+// The rotation-side FP16 operands of the likelihood from the slices S.
+static int estep_operands(emc_plan* p) {
   emc_ctx* ctx = p->ctx;
   TcState* st = state(p);
   const size_t rk = (size_t)p->Rp * p->Kp;
-  int rc;
+  if (p->d.diff == EMC_DIFF_TRUE_POISSON) {
+    tc_rot_logs_kernel<<<ctx->sm_count * 8, 256, 0, ctx->stream>>>(p->S, rk, st->Gh, st->Gl);
+    return after_launch(ctx, "tc_rot_logs_kernel");
+  }
   tc_rot_ops_kernel<<<ctx->sm_count * 8, 256, 0, ctx->stream>>>(p->S, rk, st->Mp, st->MSh, st->Gh,
                                                                 st->Gl, st->Hh, st->Hl, p->flags);
-  if ((rc = after_launch(ctx, "tc_rot_ops_kernel"))) return rc;
+  return after_launch(ctx, "tc_rot_ops_kernel");
+}
+
+static int estep_launch(emc_plan* p, int raster, int first, int count, bool full) {
+  if (p->d.diff == EMC_DIFF_TRUE_POISSON) return estep_pois_launch(p, raster, first, count, full);
+  emc_ctx* ctx = p->ctx;
+  TcState* st = state(p);
   TcEstepArgs a;
   a.N = p->d.n_images;
   a.R = p->d.n_rot;
@@ -1038,10 +1069,11 @@ int tc_estep(emc_plan* p) {
   a.n_pt = p->Np / es::BM;
   a.n_rt = p->Rp / es::BN;
   a.nkb = p->Kp / es::BK;
+  a.raster = raster;
   // auto: G lo always; H lo too when the intensity is known (phi = 1 leaves
   // the C = K^2 . H term unbalanced, and its rounding shows in the likelihood)
   a.gh_lo = p->estep_gh_lo >= 0 ? p->estep_gh_lo : (p->d.known_intensity ? 3 : 1);
-  a.tiles = p->prune_tiles;
+  a.tiles = full ? nullptr : p->prune_tiles;
   a.k2lo_any = p->k2lo_any;
   a.k2_inv = 1.0f / p->k2_scale;
   a.rot_cnt = p->rot_cnt;
@@ -1056,7 +1088,10 @@ int tc_estep(emc_plan* p) {
   a.bad = p->flags + 4;
   a.status = st->status;
   const CUtensorMap* rm = st->rot;
-  const int grid = p->prune_tiles ? p->prune_n_tiles : a.n_pt * a.n_rt;
+  const int total = a.n_pt * a.n_rt;
+  first = a.tiles ? 0 : std::max(0, std::min(first, total));
+  const int grid = a.tiles ? p->prune_n_tiles : std::min(total - first, count);
+  a.tile0 = first;
   if (grid == 0) return EMC_OK;
   tc_estep_kernel<<<grid, es::THREADS, es::SMEM_BYTES, ctx->stream>>>(
       st->mK, st->mK2h, st->mK2l, rm[0], rm[1], rm[2], rm[3], rm[4], rm[5], a);
@@ -1064,6 +1099,93 @@ int tc_estep(emc_plan* p) {
   if (e != cudaSuccess) return cuda_fail(ctx, e, "tc_estep_kernel launch");
   return after_launch(ctx, "tc_estep_kernel");
 }
+
+int tc_estep(emc_plan* p) {
+  int rc = estep_operands(p);
+  if (rc) return rc;
+  return estep_launch(p, p->estep_raster, 0, INT_MAX, false);
+}
+
+// One timed launch of the likelihood kernel over tiles [first, first + count)
+// of the order `raster` (CUDA events on the plan's stream; synchronises).  The
+// rotation operands are those of the last expansion.
+int tc_time_estep(emc_plan* p, int raster, int first, int count, float* ms) {
+  emc_ctx* ctx = p->ctx;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  EMC_CUDA(ctx, cudaEventCreate(&e0));
+  cudaError_t ce = cudaEventCreate(&e1);
+  int rc = EMC_OK;
+  if (ce == cudaSuccess) ce = cudaEventRecord(e0, ctx->stream);
+  if (ce == cudaSuccess && !(rc = estep_launch(p, raster, first, count, true)))
+    ce = cudaEventRecord(e1, ctx->stream);
+  if (ce == cudaSuccess && !rc) ce = cudaEventSynchronize(e1);
+  if (ce == cudaSuccess && !rc) ce = cudaEventElapsedTime(ms, e0, e1);
+  if (ce != cudaSuccess && !rc) rc = cuda_fail(ctx, ce, "likelihood timing");
+  cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  return rc;
+}
+
+int tc_estep_tiles(emc_plan* p) {
+  const int n_pt = p->Np / 128;
+  const int n_rt = p->d.diff == EMC_DIFF_TRUE_POISSON ? ceil_div(p->Rp, ep::BN) : p->Rp / es::BN;
+  return n_pt * n_rt;
+}
+
+// Raster autotuner.  The likelihood kernel streams two operand panels per
+// CTA (the pattern tile's and the rotation tile's, 128 rows x the compacted
+// pixel count each); which CTAs run side by side decides how often a panel
+// is served from L2 rather than HBM, and the best order depends on the panel
+// length and the tile counts: on 256^3 workloads (51,020 pixels) groups of 4
+// rotation tiles run at 5.7 ms per 1,000 tiles while groups of 8 swing
+// between 5.5 and 10.3 ms depending on where in the grid they are timed; at
+// 128^3 all orders are within 5 %.  Candidates: groups of 2..16 rotation
+// tiles, or of 8..76 pattern tiles.  Each is timed on two windows of `waves`
+// x SM-count tiles inside the grid (at 30 % and 65 % of its order; the whole
+// grid when it is smaller) and scored by the slower window, so an order that
+// is fast only at times loses to a steady one.  The rotation operands are
+// rebuilt from the slices of the last expansion; the timed launches
+// overwrite responsibilities and scaling of the tiles they cover.
+int tc_autotune(emc_plan* p, int waves, int* best, float* best_ms) {
+  emc_ctx* ctx = p->ctx;
+  int rc = estep_operands(p);
+  if (rc) return rc;
+  const bool pois = p->d.diff == EMC_DIFF_TRUE_POISSON;
+  const int n_pt = p->Np / 128;
+  const int n_rt = pois ? ceil_div(p->Rp, ep::BN) : p->Rp / es::BN;
+  const int total = n_pt * n_rt;
+  const int count = std::min(total, std::max(1, waves) * ctx->sm_count);
+  std::vector<int> firsts;
+  if (count >= total) {
+    firsts.push_back(0);
+  } else {
+    for (double f : {0.30, 0.65})
+      firsts.push_back(std::min(total - count, (int)(f * total)));
+  }
+  std::vector<int> cand;
+  for (int g : {8, 2, 4, 16, -8, -19, -38, -76}) {
+    const int c = g > 0 ? std::min(g, n_rt) : -std::min(-g, n_pt);
+    if (std::find(cand.begin(), cand.end(), c) == cand.end()) cand.push_back(c);
+  }
+  std::vector<float> t(cand.size(), 0.0f);
+  for (size_t j = 0; j < cand.size() && !rc; ++j) {
+    for (int first : firsts) {
+      float ms = 0.0f;
+      if ((rc = tc_time_estep(p, cand[j], first, count, &ms))) break;
+      t[j] = std::max(t[j], ms);
+    }
+  }
+  if (rc) return rc;
+  size_t b = 0;
+  for (size_t j = 1; j < cand.size(); ++j)
+    if (t[j] < t[b]) b = j;
+  p->estep_raster = cand[b];
+  if (best) *best = cand[b];
+  if (best_ms) *best_ms = t[b];
+  return EMC_OK;
+}
+
+int tc_estep_prepare(emc_plan* p) { return estep_operands(p); }
 
 int tc_mstep(emc_plan* p, float* model, float* weight) {
   emc_ctx* ctx = p->ctx;

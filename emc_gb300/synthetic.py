@@ -274,4 +274,11 @@ def _render_torch(model, tq, pts, mask, scales, cfg, device):
     lam *= torch.as_tensor(scales, device=device, dtype=torch.float32)[:, None]
     gen = torch.Generator(device=device)
     gen.manual_seed(cfg.seed + 12345)
-    return torch.poisson(lam, generator=gen).cpu().numpy().astype(np.float32)
+    # one Poisson draw per chunk of fewer than 2^31 elements: a single draw over
+    # the 256^3 workload's 6.6e9 elements left part of its output unwritten
+    step = max(1, (2 ** 31 - 1) // (s * s))
+    out = np.empty((N, s * s), np.float32)
+    for i0 in range(0, N, step):
+        i1 = min(N, i0 + step)
+        out[i0:i1] = torch.poisson(lam[i0:i1], generator=gen).cpu().numpy()
+    return out

@@ -392,7 +392,32 @@ int emc_batch_destroy(emc_batch* batch);
  * above 2048 are rounded to the nearest FP16 value (relative error <= 2^-12,
  * only at those pixels).  Set before emc_plan_bind. */
 #define EMC_OPT_COUNTS_ROUND 5
+/* EMC_OPT_ESTEP_RASTER: order of the likelihood kernel's (pattern tile,
+ * rotation tile) CTAs.  g > 0 (default 8): groups of g rotation tiles, each
+ * group running through all pattern tiles; g < 0: groups of -g pattern tiles
+ * running through all rotation tiles.  |g| <= 4096.  Results do not depend on
+ * it; L2 reuse of the operand panels does. */
+#define EMC_OPT_ESTEP_RASTER 6
 int emc_plan_set_option(emc_plan* plan, int option, int value);
+/* Tile-order autotuner of the tensor-core likelihood kernel: expands d_model
+ * (sigma as in emc_iterate), times the kernel for each candidate
+ * EMC_OPT_ESTEP_RASTER order on two windows of 256 waves of the SMs inside
+ * its tile grid (the whole grid when smaller), scores each order by its
+ * slower window and sets the fastest; *h_raster / *h_ms (may be NULL)
+ * receive it and that time.  Synchronous.  Overwrites the plan's responsibilities and scaling
+ * (the next emc_iterate rewrites them); d_model is not changed.  FP32 plans
+ * have no tile order: *h_raster = 0.  Results of later iterations do not
+ * depend on the order. */
+int emc_plan_autotune(emc_plan* plan, const float* d_model, float sigma, int* h_raster,
+                      float* h_ms);
+/* Times one launch of the tensor-core likelihood kernel over tiles
+ * [first_tile, first_tile + n_tiles) of the order `raster` (clipped to the
+ * grid; CUDA events, synchronous) into *h_ms, and the grid's tile count into
+ * *h_total_tiles (may be NULL).  d_model != NULL expands it first (sigma as
+ * in emc_iterate); NULL reuses the operands of the last expansion.
+ * Overwrites responsibilities and scaling of the covered tiles. */
+int emc_plan_time_likelihood(emc_plan* plan, const float* d_model, float sigma, int raster,
+                             int first_tile, int n_tiles, float* h_ms, int* h_total_tiles);
 /* Instrumentation: with profiling on, emc_iterate records CUDA events on the
  * context stream between its phases; emc_plan_phase_ms (after the iteration
  * completes) returns the durations of expand, E-step (scaling + likelihood),

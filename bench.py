@@ -64,6 +64,9 @@ def parse():
                          "(relative change <= 2^-12 on those pixels); without it such "
                          "patterns run on the FP32 path.  -1: on for the large configuration "
                          "(FP16 counts by its definition), off otherwise")
+    ap.add_argument("--learned-epochs", type=int, default=-1,
+                    help="learned rotation proposal leg: training epochs (0: skip; -1: 30 for "
+                         "the large configuration, 0 otherwise)")
     ap.add_argument("--raster", type=int, default=0,
                     help="tensor path: the likelihood kernel's tile order (EMC_OPT_ESTEP_RASTER); "
                          "0 (default): chosen by emc_plan_autotune before the warm-up")
@@ -79,6 +82,8 @@ def parse():
     args = ap.parse_args()
     if args.counts_round < 0:
         args.counts_round = int(args.config == "large")
+    if args.learned_epochs < 0:
+        args.learned_epochs = 30 if args.config == "large" else 0
     return args
 
 
@@ -369,6 +374,12 @@ def run_ours(args):
         plan.close()  # the prune leg's plans need the device memory
         torch.cuda.synchronize()
         pruned = prune_leg(args, prob, ctx, T, (images, mask, x, y, z, rot, w), pairs)
+    if precision == "mixed" and args.learned_epochs > 0 and rank == 0:
+        if args.prune_steps <= 0:
+            plan.close()
+            torch.cuda.synchronize()
+        pruned = dict(pruned or {}, learned=learned_leg(args, prob, ctx, T,
+                                                        (images, mask, x, y, z, rot, w)))
     return finish(args, prob, workspace, ctx, ws, rank, precision, value, ms_step, st, plain, e2e,
                   estep_ms, phases, launches, clocks, pairs, pruned, tuning)
 
@@ -435,6 +446,88 @@ def prune_leg(args, prob, ctx, T, inputs, pairs):
             "pruned_iterations": info["pruned_iterations"],
             "fallback_iterations": info["fallback_iterations"],
             "full_iterations": info["full_iterations"], "estep_raster": raster,
+            "model_rel_l2_vs_full_scan": float(np.linalg.norm(mp - mf) / np.linalg.norm(mf))}
+
+
+def learned_leg(args, prob, ctx, T, inputs):
+    """The learned rotation proposal: labels are the most probable rotations
+    of one full-scan iteration (counts x log-slice likelihood, from the true
+    particle); the network is trained on those patterns (GPU kernels of the
+    library), then predicts a held-out set of as many new patterns of the
+    same particle, whose first iteration is seeded by the proposals (2 % ball
+    around the prediction and its Friedel mate, margin, probe tiles) and timed
+    against its full scan.  Reports training time, held-out angular errors
+    against the true orientations, the seeded tile share, whether the
+    fallback ran and the model's distance to the full scan."""
+    import numpy as np
+    import torch
+
+    import emc_gb300 as E
+    from emc_gb300 import synthetic as S
+    s, R, N = prob.cfg.side, prob.quats.shape[0], prob.images.shape[0]
+    images, mask, x, y, z, rot, w = inputs
+
+    def plan_on(images):
+        p = E.Plan(ctx, s, N, R, diff=E.DIFF_TRUE_POISSON, precision=E.PREC_MIXED)
+        if args.counts_round:
+            p.set_option(E.Plan.OPT_COUNTS_ROUND, 1)
+        p.bind(images, mask, x, y, z, rot, w)
+        return p
+    m0 = T(prob.true_model)
+    ctx.normalize_model(s, m0)
+    plan = plan_on(images)
+    m, wt = m0.clone(), torch.empty_like(m0)
+    plan.iterate(m, wt, 0.12, stats=False)
+    labels = torch.empty((N, 4), device=m0.device)
+    plan.best_quaternions(labels)
+    plan.close()
+    net = E.Proposal(ctx, seed=1)
+    net.set_data(images, mask, s)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    losses = net.train(labels, epochs=args.learned_epochs, batch=128, lr=1e-3, seed=1)
+    train_s = time.perf_counter() - t0
+    held = S.make_problem(prob.cfg, device="cuda", pattern_seed=1)
+    torch.cuda.empty_cache()
+    himages = T(held.images)
+    net.set_data(himages, mask, s, fit_stats=False)
+    props = net.predict(torch.empty((N, 2, 4), device=m0.device))
+    net.close()
+    pq = props.cpu().numpy().astype(np.float64)
+    tq = held.true_quats
+    err = np.degrees(2 * np.arccos(np.clip(np.maximum(np.abs((pq[:, 0] * tq).sum(1)),
+                                                      np.abs((pq[:, 1] * tq).sum(1))), 0, 1)))
+    runs = {}
+    for kind in ("full", "seeded"):
+        plan = plan_on(himages)
+        if args.raster:
+            plan.set_option(E.Plan.OPT_ESTEP_RASTER, args.raster)
+        seeded = None
+        if kind == "seeded":
+            plan.set_pruning(True, min_mass=0.999, dilate=1.0)
+            plan.set_proposals(props, 0.02, 16)
+            seeded = plan.prune_info()["active_fraction"]
+        m = m0.clone()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        plan.iterate(m, wt, 0.12, stats=False)  # ends with a synchronise
+        dt = time.perf_counter() - t0
+        info = plan.prune_info() if kind == "seeded" else None
+        runs[kind] = (dt, m.cpu().numpy().astype(np.float64), info, seeded)
+        plan.close()
+        torch.cuda.synchronize()
+    tf, mf, _, _ = runs["full"]
+    tp, mp, info, seeded = runs["seeded"]
+    return {"network": "4 conv 3x3/2 (64 ch) + linear to 6D, FP32, trained on the GPU",
+            "train_patterns": N, "epochs": args.learned_epochs,
+            "train_s": train_s, "loss_first_last": [float(losses[0]), float(losses[-1])],
+            "heldout_patterns": N,
+            "heldout_err_deg_median": float(np.median(err)),
+            "heldout_err_deg_p90": float(np.percentile(err, 90)),
+            "heldout_within_2pct_ball": float((err < 41.8).mean()),
+            "seeded_active_fraction": seeded, "fallback": bool(info["fallback"]),
+            "margin_mass": info["margin_mass"],
+            "first_iteration_ms": {"full_scan": tf * 1e3, "seeded": tp * 1e3},
             "model_rel_l2_vs_full_scan": float(np.linalg.norm(mp - mf) / np.linalg.norm(mf))}
 
 

@@ -361,6 +361,23 @@ class Plan:
                         "plan_pattern_order")
         return out
 
+    def best_quaternions(self, out):
+        """The most probable rotation of every pattern in the last
+        iteration's responsibilities: out [N][4] float32 CUDA tensor, input
+        pattern order (emc_plan_best_quaternions)."""
+        self.ctx._check(self._lib.emc_plan_best_quaternions(self._h, _ptr(out, name="out")),
+                        "plan_best_quaternions")
+        return out
+
+    def set_proposals(self, quats, fraction: float = 0.02, probe_stride: int = 16):
+        """Seeds the next pruned iteration from rotation proposals quats
+        [N][modes][4] (emc_plan_set_proposals)."""
+        if quats.dim() != 3 or quats.shape[2] != 4 or quats.shape[0] != self.desc.n_images:
+            raise EmcError("proposals must be [n_images][modes][4]")
+        self.ctx._check(self._lib.emc_plan_set_proposals(
+            self._h, _ptr(quats, name="quats"), int(quats.shape[1]), float(fraction),
+            int(probe_stride)), "plan_set_proposals")
+
     def rotation_order(self):
         """Input rotation index of each row of the last iteration's results."""
         out = np.zeros(self.desc.n_rot, np.int32)
@@ -441,6 +458,102 @@ class Plan:
     def close(self):
         if getattr(self, "_h", None):
             self._lib.emc_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Proposal:
+    """The learned rotation proposal network (emc_proposal_* in the C ABI):
+    trained on the GPU on EMC's most probable rotations, it predicts each
+    pattern's rotation and its Friedel mate."""
+
+    def __init__(self, ctx: Context, seed: int = 0):
+        self.ctx = ctx
+        self._lib = ctx._lib
+        h = C.c_void_p()
+        ctx._check(self._lib.emc_proposal_create(ctx._h, int(seed), C.byref(h)), "proposal_create")
+        self._h = h
+        self.n_params = int(self._lib.emc_proposal_param_count(h))
+        self.n_data = 0
+        ctx._children.add(self)
+
+    def params(self) -> np.ndarray:
+        out = np.empty(self.n_params, np.float32)
+        self.ctx._check(self._lib.emc_proposal_params(self._h, out.ctypes.data, 1),
+                        "proposal_params")
+        return out
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, np.float32)
+        if p.size != self.n_params:
+            raise EmcError(f"expected {self.n_params} parameters")
+        self.ctx._check(self._lib.emc_proposal_params(self._h, p.ctypes.data, 0),
+                        "proposal_params")
+
+    def set_data(self, images, mask, side: int, fit_stats: bool = True):
+        """Bins the patterns images [N][side^2] (mask [side^2] int32) into
+        the network's input rows, standardised per input pixel with
+        statistics fitted on these patterns (fit_stats) or the stored ones."""
+        n = images.shape[0]
+        self.ctx._check(self._lib.emc_proposal_set_data(
+            self._h, _ptr(images, name="images"), _ptr(mask, name="mask"), int(side), int(n),
+            int(bool(fit_stats))), "proposal_set_data")
+        self.n_data = n
+
+    def stats(self) -> np.ndarray:
+        """Input statistics [2][4096]: per-pixel mean and 1 / spread."""
+        out = np.empty((2, 4096), np.float32)
+        self.ctx._check(self._lib.emc_proposal_stats(self._h, out.ctypes.data, 1),
+                        "proposal_stats")
+        return out
+
+    def inputs(self, first: int, count: int) -> np.ndarray:
+        out = np.empty((count, 4096), np.float32)
+        self.ctx._check(self._lib.emc_proposal_inputs(self._h, int(first), int(count),
+                                                      out.ctypes.data), "proposal_inputs")
+        return out
+
+    def loss_grad(self, rows, quats):
+        """Mean loss and parameter gradient of one batch (rows of the data,
+        labels quats [N][4] CUDA float32)."""
+        rows = np.ascontiguousarray(rows, np.int32)
+        loss = C.c_float(0.0)
+        g = np.empty(self.n_params, np.float32)
+        self.ctx._check(self._lib.emc_proposal_loss_grad(
+            self._h, rows.ctypes.data, int(rows.size), _ptr(quats, name="quats"), C.byref(loss),
+            g.ctypes.data), "proposal_loss_grad")
+        return loss.value, g
+
+    def train(self, quats, rows=None, epochs: int = 10, batch: int = 256, lr: float = 1e-3,
+              seed: int = 0, augment: bool = True) -> np.ndarray:
+        """Adam over shuffled minibatches (augment: random in-plane quarter
+        turns); returns each epoch's mean loss."""
+        losses = np.zeros(max(epochs, 1), np.float32)
+        if rows is None:
+            rp, nr = None, 0
+        else:
+            rows = np.ascontiguousarray(rows, np.int32)
+            rp, nr = rows.ctypes.data, int(rows.size)
+        self.ctx._check(self._lib.emc_proposal_train(
+            self._h, _ptr(quats, name="quats"), rp, nr, int(epochs), int(batch), float(lr),
+            int(seed), int(bool(augment)), losses.ctypes.data), "proposal_train")
+        return losses[:epochs]
+
+    def predict(self, out):
+        """out [N][2][4] CUDA float32: each pattern's predicted rotation and
+        its Friedel mate (quaternions, w >= 0)."""
+        self.ctx._check(self._lib.emc_proposal_predict(self._h, _ptr(out, name="out")),
+                        "proposal_predict")
+        return out
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.emc_proposal_destroy(self._h)
             self._h = None
 
     def __del__(self):

@@ -133,6 +133,18 @@ SIGNATURES: dict[str, tuple] = {
     "emc_plan_prune_info": (I, [P, C.POINTER(PruneInfo)]),
     "emc_plan_pattern_order": (I, [P, P]),
     "emc_plan_rotation_order": (I, [P, P]),
+    "emc_plan_best_quaternions": (I, [P, P]),
+    "emc_plan_set_proposals": (I, [P, P, I, F, I]),
+    "emc_proposal_create": (I, [P, C.c_ulonglong, C.POINTER(P)]),
+    "emc_proposal_destroy": (I, [P]),
+    "emc_proposal_param_count": (I, [P]),
+    "emc_proposal_params": (I, [P, P, I]),
+    "emc_proposal_set_data": (I, [P, P, P, I, I, I]),
+    "emc_proposal_stats": (I, [P, P, I]),
+    "emc_proposal_inputs": (I, [P, I, I, P]),
+    "emc_proposal_loss_grad": (I, [P, P, I, P, C.POINTER(F), P]),
+    "emc_proposal_train": (I, [P, P, P, I, I, I, F, C.c_ulonglong, I, P]),
+    "emc_proposal_predict": (I, [P, P]),
     "emc_batch_create": (I, [P, P, P, I, C.POINTER(P)]),
     "emc_batch_run": (I, [P, P]),
     "emc_batch_wait": (I, [P, P]),

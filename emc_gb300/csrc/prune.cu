@@ -39,6 +39,7 @@ struct PruneState {
   std::vector<int> h_perm;          // position -> input pattern, of the operands
   std::vector<int> h_perm_results;  // the same, of the last iteration's results
   int *d_perm = nullptr, *d_newpos = nullptr, *d_best = nullptr;
+  int* d_perm_res = nullptr;  // h_perm_results on the device (emc_plan_best_quaternions)
   unsigned char *d_core = nullptr, *d_state = nullptr, *d_adj = nullptr;
   int2* d_tiles = nullptr;
   int n_tiles = 0;
@@ -149,6 +150,79 @@ __global__ void dilate_kernel(const unsigned char* __restrict__ core,
   state[e] = s;
 }
 
+// The most probable rotation's quaternion of each pattern (responsibilities
+// P [R][N] over the plan's rotation rows), written at the pattern's input
+// index perm[i] (perm: column -> input pattern; nullptr: identity).
+__global__ void best_quat_kernel(const float* __restrict__ P, int R, int N,
+                                 const float* __restrict__ rot, const int* __restrict__ perm,
+                                 float* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  float bv = -1.0f;
+  int br = 0;
+  for (int r = 0; r < R; ++r) {
+    const float v = P[(size_t)r * N + i];
+    if (v > bv) {
+      bv = v;
+      br = r;
+    }
+  }
+  const int d = perm ? perm[i] : i;
+  for (int c = 0; c < 4; ++c) out[4 * (size_t)d + c] = rot[4 * (size_t)br + c];
+}
+
+// nearest[i] = the rotation row closest to pattern i's first proposal
+// (props [N][n_modes][4]).  Rotations staged through shared memory.
+__global__ void nearest_row_kernel(const float* __restrict__ props, int n_modes,
+                                   const float* __restrict__ rot, int R, int N,
+                                   int* __restrict__ nearest) {
+  __shared__ float4 sq[512];
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  float4 q = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  if (i < N) q = load_q(props, i * n_modes);
+  float bv = -1.0f;
+  int br = 0;
+  for (int r0 = 0; r0 < R; r0 += 512) {
+    __syncthreads();
+    for (int r = threadIdx.x; r < 512 && r0 + r < R; r += blockDim.x) sq[r] = load_q(rot, r0 + r);
+    __syncthreads();
+    const int r1 = min(512, R - r0);
+    for (int r = 0; r < r1; ++r) {
+      const float v = qdot(q, sq[r]);
+      if (v > bv) {
+        bv = v;
+        br = r0 + r;
+      }
+    }
+  }
+  if (i < N) nearest[i] = br;
+}
+
+// core[newpos[i] / 128][rt] = 1 when some rotation of tile rt lies within the
+// ball (half-angle cosine cos_half) around one of pattern i's proposals.
+__global__ void proposal_core_kernel(const float* __restrict__ props, int n_modes,
+                                     const float* __restrict__ rot, int R, int N,
+                                     const int* __restrict__ newpos, float cos_half, int n_rt,
+                                     unsigned char* __restrict__ core) {
+  __shared__ float4 sq[128];
+  const int rt = blockIdx.y;
+  const int r0 = rt * 128, cnt = min(128, R - r0);
+  for (int r = threadIdx.x; r < cnt; r += blockDim.x) sq[r] = load_q(rot, r0 + r);
+  __syncthreads();
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  bool hit = false;
+  for (int m = 0; m < n_modes && !hit; ++m) {
+    const float4 q = load_q(props, i * n_modes + m);
+    for (int r = 0; r < cnt; ++r)
+      if (qdot(q, sq[r]) >= cos_half) {
+        hit = true;
+        break;
+      }
+  }
+  if (hit) core[(size_t)(newpos[i] >> 7) * n_rt + rt] = 1;
+}
+
 static int prune_alloc(emc_plan* p, PruneState* ps) {
   const int N = p->d.n_images, R = p->d.n_rot, n_rt = p->n_rt, n_pt = p->Np / 128;
   const size_t n3 = (size_t)p->d.side * p->d.side * p->d.side;
@@ -156,6 +230,7 @@ static int prune_alloc(emc_plan* p, PruneState* ps) {
   if (!rc) rc = plan_alloc(p, (void**)&ps->d_perm, sizeof(int) * N);
   if (!rc) rc = plan_alloc(p, (void**)&ps->d_newpos, sizeof(int) * N);
   if (!rc) rc = plan_alloc(p, (void**)&ps->d_best, sizeof(int) * N);
+  if (!rc) rc = plan_alloc(p, (void**)&ps->d_perm_res, sizeof(int) * N);
   if (!rc) rc = plan_alloc(p, (void**)&ps->d_core, (size_t)n_pt * n_rt);
   if (!rc) rc = plan_alloc(p, (void**)&ps->d_state, (size_t)n_pt * n_rt);
   if (!rc) rc = plan_alloc(p, (void**)&ps->d_adj, (size_t)n_rt * n_rt);
@@ -256,6 +331,9 @@ static int prune_geometry(emc_plan* p, PruneState* ps) {
 // Masks and tile list for the next iteration from the responsibilities of
 // the last one (p->L, operands in ps->h_perm order); with reorder, the
 // patterns are first re-sorted by their most probable rotation.
+static int prune_finish(emc_plan* p, PruneState* ps, const std::vector<int>& new_perm,
+                        int probe_stride = 0, bool arm = false);
+
 static int prune_prepare(emc_plan* p, PruneState* ps, bool reorder) {
   emc_ctx* ctx = p->ctx;
   const int N = p->d.n_images, R = p->d.n_rot, n_rt = p->n_rt, n_pt = p->Np / 128;
@@ -282,6 +360,21 @@ static int prune_prepare(emc_plan* p, PruneState* ps, bool reorder) {
   tile_mass_kernel<<<dim3(ceil_div(N, 256), n_rt), 256, 0, ctx->stream>>>(
       p->L, R, N, n_rt, ps->d_newpos, ps->tau, ps->d_core);
   if ((rc = after_launch(ctx, "tile_mass_kernel"))) return rc;
+  return prune_finish(p, ps, new_perm);
+}
+
+// From the core tiles in ps->d_core (rows: pattern tiles of the order
+// new_perm): margin dilation, tile lists of both kernels, the pattern-side
+// operands in the new order, and whether the next iteration is pruned.
+// probe_stride > 0 adds, as margin, every probe_stride-th rotation tile of
+// each pattern tile (staggered by pattern tile): mass found there also
+// repeats the iteration as a full scan.  arm: the next iteration is pruned
+// however dense the tile set (else only below 75 % of the tiles).
+static int prune_finish(emc_plan* p, PruneState* ps, const std::vector<int>& new_perm,
+                        int probe_stride, bool arm) {
+  emc_ctx* ctx = p->ctx;
+  const int N = p->d.n_images, n_rt = p->n_rt, n_pt = p->Np / 128;
+  int rc;
   dilate_kernel<<<ceil_div(n_pt * n_rt, 256), 256, 0, ctx->stream>>>(ps->d_core, ps->d_adj, n_pt,
                                                                      n_rt, ps->d_state);
   if ((rc = after_launch(ctx, "dilate_kernel"))) return rc;
@@ -289,6 +382,15 @@ static int prune_prepare(emc_plan* p, PruneState* ps, bool reorder) {
   EMC_CUDA(ctx, cudaMemcpyAsync(state.data(), ps->d_state, state.size(), cudaMemcpyDeviceToHost,
                                 ctx->stream));
   EMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  if (probe_stride > 0) {
+    for (int pt = 0; pt < n_pt; ++pt)
+      for (int rt = pt % probe_stride; rt < n_rt; rt += probe_stride) {
+        unsigned char& st = state[(size_t)pt * n_rt + rt];
+        if (!st) st = 2;
+      }
+    EMC_CUDA(ctx, cudaMemcpyAsync(ps->d_state, state.data(), state.size(), cudaMemcpyHostToDevice,
+                                  ctx->stream));
+  }
   // The true-Poisson E-step evaluates 256 rotations per CTA: both 128-row
   // halves of a pair take the stronger state, so that every evaluated row is
   // also counted by the normalisation.
@@ -349,8 +451,8 @@ static int prune_prepare(emc_plan* p, PruneState* ps, bool reorder) {
   }
   EMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));  // host vectors above are staged
   // a dense mask is cheaper as a full scan
-  ps->ready = ps->info.active_fraction < 0.75 &&
-              !(ps->full_every > 0 && ps->since_full + 1 >= ps->full_every);
+  ps->ready = arm || (ps->info.active_fraction < 0.75 &&
+                      !(ps->full_every > 0 && ps->since_full + 1 >= ps->full_every));
   return EMC_OK;
 }
 
@@ -515,4 +617,68 @@ extern "C" int emc_plan_rotation_order(emc_plan* p, int* order) {
   PruneState* ps = pstate(p);
   for (int r = 0; r < p->d.n_rot; ++r) order[r] = ps ? ps->h_rorder[r] : r;
   return EMC_OK;
+}
+
+extern "C" int emc_plan_best_quaternions(emc_plan* p, float* d_quats) {
+  if (!p) return EMC_ERR_INVALID;
+  emc_ctx* ctx = p->ctx;
+  EMC_REQUIRE(ctx, p->bound && d_quats, "best_quaternions: plan not bound or null output");
+  const int N = p->d.n_images, R = p->d.n_rot;
+  PruneState* ps = pstate(p);
+  const int* perm = nullptr;
+  if (ps) {
+    EMC_CUDA(ctx, cudaMemcpyAsync(ps->d_perm_res, ps->h_perm_results.data(), sizeof(int) * N,
+                                  cudaMemcpyHostToDevice, ctx->stream));
+    perm = ps->d_perm_res;
+  }
+  best_quat_kernel<<<ceil_div(N, 256), 256, 0, ctx->stream>>>(p->L, R, N, p->rot, perm, d_quats);
+  int rc = after_launch(ctx, "best_quat_kernel");
+  if (!rc) EMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));  // the host perm is staged
+  return rc;
+}
+
+// Fraction of the rotation group SO(3) (uniform measure) within angle theta
+// of a rotation: (theta - sin theta) / pi.
+static double ball_angle(double fraction) {
+  double lo = 0.0, hi = M_PI;
+  for (int it = 0; it < 100; ++it) {
+    const double mid = 0.5 * (lo + hi);
+    if ((mid - std::sin(mid)) / M_PI < fraction)
+      lo = mid;
+    else
+      hi = mid;
+  }
+  return 0.5 * (lo + hi);
+}
+
+extern "C" int emc_plan_set_proposals(emc_plan* p, const float* d_quats, int n_modes,
+                                      float fraction, int probe_stride) {
+  if (!p) return EMC_ERR_INVALID;
+  emc_ctx* ctx = p->ctx;
+  PruneState* ps = pstate(p);
+  EMC_REQUIRE(ctx, ps && p->bound, "set_proposals: pruning is off or the plan is not bound");
+  EMC_REQUIRE(ctx, d_quats && n_modes >= 1 && n_modes <= 8 && fraction > 0.0f &&
+                       fraction < 1.0f && probe_stride >= 0,
+              "set_proposals: bad arguments");
+  const int N = p->d.n_images, R = p->d.n_rot, n_rt = p->n_rt, n_pt = p->Np / 128;
+  const float cos_half = (float)std::cos(0.5 * ball_angle((double)fraction));
+  int rc;
+  // patterns sorted by the rotation row nearest to their first proposal
+  nearest_row_kernel<<<ceil_div(N, 256), 256, 0, ctx->stream>>>(d_quats, n_modes, p->rot, R, N,
+                                                                ps->d_best);
+  if ((rc = after_launch(ctx, "nearest_row_kernel"))) return rc;
+  std::vector<int> best(N), order(N), newpos(N);
+  EMC_CUDA(ctx, cudaMemcpyAsync(best.data(), ps->d_best, sizeof(int) * N, cudaMemcpyDeviceToHost,
+                                ctx->stream));
+  EMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return best[a] < best[b]; });
+  for (int j = 0; j < N; ++j) newpos[order[j]] = j;
+  EMC_CUDA(ctx, cudaMemcpyAsync(ps->d_newpos, newpos.data(), sizeof(int) * N,
+                                cudaMemcpyHostToDevice, ctx->stream));
+  EMC_CUDA(ctx, cudaMemsetAsync(ps->d_core, 0, (size_t)n_pt * n_rt, ctx->stream));
+  proposal_core_kernel<<<dim3(ceil_div(N, 128), n_rt), 128, 0, ctx->stream>>>(
+      d_quats, n_modes, p->rot, R, N, ps->d_newpos, cos_half, n_rt, ps->d_core);
+  if ((rc = after_launch(ctx, "proposal_core_kernel"))) return rc;
+  return prune_finish(p, ps, order, probe_stride, true);  // order: position -> input pattern
 }

@@ -163,11 +163,14 @@ class Problem:
     scales: np.ndarray       # float64 [N]
 
 
-def make_problem(cfg: Config, device: str | None = None, coords=None, rotations=None) -> Problem:
+def make_problem(cfg: Config, device: str | None = None, coords=None, rotations=None,
+                 pattern_seed: int | None = None) -> Problem:
     """Builds the problem.  `coords` = (x, y, z) and `rotations` = (quats,
     weights) come from the library's host functions (emc_calculate_coordinates,
     emc_generate_rotations) unless given.  `device` = "cuda" renders the
-    patterns with torch on the GPU (same numbers up to float rounding)."""
+    patterns with torch on the GPU (same numbers up to float rounding).
+    `pattern_seed` draws new orientations, scales, counts and initial model
+    for the same particle and detector (a held-out set)."""
     rng = np.random.default_rng(cfg.seed)
     s = cfg.side
     true = particle_intensity(s, cfg.n_atoms, cfg.atom_sigma, cfg.radius, rng)
@@ -180,6 +183,8 @@ def make_problem(cfg: Config, device: str | None = None, coords=None, rotations=
     x, y, z = coords
     quats, weights = rotations
     mask = detector_mask(s, cfg.beamstop, cfg.masked_fraction, rng)
+    if pattern_seed is not None:
+        rng = np.random.default_rng([cfg.seed, 7919, pattern_seed])
     N = cfg.n_images
     tq = random_quaternions(N, rng)
     scales = rng.uniform(cfg.scale[0], cfg.scale[1], N)
@@ -194,7 +199,8 @@ def make_problem(cfg: Config, device: str | None = None, coords=None, rotations=
         lam *= (cfg.photons / lam.sum(1, dtype=np.float64).mean()) * scales[:, None]
         images = rng.poisson(lam).astype(np.float32)
     else:
-        images = _render_torch(true.reshape(s, s, s), tq, pts, mask, scales, cfg, device)
+        images = _render_torch(true.reshape(s, s, s), tq, pts, mask, scales, cfg, device,
+                               0 if pattern_seed is None else 1000003 * (pattern_seed + 1))
     init = rng.random(s ** 3).astype(np.float32)
     return Problem(cfg, true.reshape(-1), init, images, mask, x, y, z, quats, weights, tq, scales)
 
@@ -252,7 +258,7 @@ isDebug = 1;
     return conf
 
 
-def _render_torch(model, tq, pts, mask, scales, cfg, device):
+def _render_torch(model, tq, pts, mask, scales, cfg, device, seed_offset=0):
     """GPU rendering of the Poisson patterns (torch; the generator is seeded)."""
     import torch
     s = model.shape[0]
@@ -273,7 +279,7 @@ def _render_torch(model, tq, pts, mask, scales, cfg, device):
     lam *= float(cfg.photons / lam.sum(1, dtype=torch.float64).mean().item())
     lam *= torch.as_tensor(scales, device=device, dtype=torch.float32)[:, None]
     gen = torch.Generator(device=device)
-    gen.manual_seed(cfg.seed + 12345)
+    gen.manual_seed(cfg.seed + 12345 + seed_offset)
     # one Poisson draw per chunk of fewer than 2^31 elements: a single draw over
     # the 256^3 workload's 6.6e9 elements left part of its output unwritten
     step = max(1, (2 ** 31 - 1) // (s * s))

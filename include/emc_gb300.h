@@ -359,6 +359,57 @@ int emc_plan_pattern_order(emc_plan* plan, int* h_order);
 /* Rotation order of the results while pruning is on (the plan keeps its
  * rotations in a spatially coherent order): row -> input rotation. */
 int emc_plan_rotation_order(emc_plan* plan, int* h_order);
+/* Learned rotation proposal (no counterpart in the reference).
+ * emc_plan_best_quaternions: the most probable rotation of every pattern in
+ * the last iteration's responsibilities, as quaternions d_quats[N][4] in the
+ * input pattern order (the network's training labels).
+ * emc_plan_set_proposals: seeds the next pruned iteration (pruning on) from
+ * per-pattern rotation proposals d_quats[N][n_modes][4] (input pattern
+ * order) instead of a previous iteration's responsibilities: the patterns
+ * are sorted by their first proposal, a rotation tile is evaluated when one
+ * of its rotations lies within the ball holding `fraction` of the rotation
+ * group around one of the pattern tile's proposals, plus the usual margin
+ * and, with probe_stride > 0, every probe_stride-th rotation tile as a probe
+ * of the rest; mass in margin and probes above 1 - min_mass repeats the
+ * iteration as a full scan.  The next iteration is pruned however dense the
+ * seeded tiles are: emc_plan_prune_info's active_fraction tells the caller,
+ * and emc_plan_set_pruning disarms it. */
+int emc_plan_best_quaternions(emc_plan* plan, float* d_quats);
+int emc_plan_set_proposals(emc_plan* plan, const float* d_quats, int n_modes, float fraction,
+                           int probe_stride);
+/* The proposal network: patterns binned to 64 x 64 (log1p of counts scaled
+ * to a mean of 1), four 3x3 stride-2 convolutions of 64 channels with ReLU,
+ * one linear layer to a 6D rotation (two matrix columns, Gram-Schmidt).
+ * Loss per pattern min(|o - t|^2, |o + t|^2), t the label's 6D form: -t is
+ * the 6D form of the Friedel mate M diag(-1, -1, 1).  Trained with Adam.
+ * emc_proposal_set_data bins the patterns (side a multiple of 64) into the
+ * network's input rows and standardises every input pixel by a mean and
+ * spread, fitted on these patterns when fit_stats = 1 (training data), else
+ * the stored ones (emc_proposal_stats gets/sets them: [2][4096], mean and
+ * 1 / spread); train/loss_grad take labels d_quats[n][4] per row; predict
+ * writes d_quats_out[n][2][4]: the prediction and its mate. */
+typedef struct emc_proposal emc_proposal;
+int emc_proposal_create(emc_ctx* ctx, unsigned long long seed, emc_proposal** out);
+int emc_proposal_destroy(emc_proposal* net);
+int emc_proposal_param_count(const emc_proposal* net);
+/* get = 1 copies the parameters to h_params, 0 sets them (and resets Adam). */
+int emc_proposal_params(emc_proposal* net, float* h_params, int get);
+int emc_proposal_set_data(emc_proposal* net, const float* d_images, const int* d_mask, int side,
+                          int n_images, int fit_stats);
+int emc_proposal_stats(emc_proposal* net, float* h_stats, int get);
+int emc_proposal_inputs(emc_proposal* net, int first, int count, float* h_out);
+/* One batch (rows h_rows[B]): mean loss and the gradient of every parameter. */
+int emc_proposal_loss_grad(emc_proposal* net, const int* h_rows, int B, const float* d_quats,
+                           float* h_loss, float* h_grads);
+/* Epochs of shuffled minibatches over h_rows[n_rows] (NULL: every row);
+ * augment = 1 turns each sample in-plane by a random multiple of 90 degrees
+ * (label composed with the matching turn about the beam axis); the Adam step
+ * size decays from lr along a cosine to 5 % of it over the call;
+ * h_epoch_loss[epochs] (may be NULL) receives each epoch's mean loss. */
+int emc_proposal_train(emc_proposal* net, const float* d_quats, const int* h_rows, int n_rows,
+                       int epochs, int batch, float lr, unsigned long long seed, int augment,
+                       float* h_epoch_loss);
+int emc_proposal_predict(emc_proposal* net, float* d_quats_out);
 /* Batched reconstructions (no counterpart in the reference): n bound plans,
  * each with its own model/weight, captured (emc_plan_capture) and nested as
  * independent child graphs of one graph; emc_batch_run launches one

@@ -67,6 +67,8 @@ def parse():
     ap.add_argument("--learned-epochs", type=int, default=-1,
                     help="learned rotation proposal leg: training epochs (0: skip; -1: 30 for "
                          "the large configuration, 0 otherwise)")
+    ap.add_argument("--estep-pair", type=int, choices=[0, 1], default=1,
+                    help="tensor path: full likelihood scans on CTA pairs (EMC_OPT_ESTEP_PAIR)")
     ap.add_argument("--raster", type=int, default=0,
                     help="tensor path: the likelihood kernel's tile order (EMC_OPT_ESTEP_RASTER); "
                          "0 (default): chosen by emc_plan_autotune before the warm-up")
@@ -281,6 +283,7 @@ def run_ours(args):
         p.set_option(E.Plan.OPT_MSTEP_AGGREGATE, args.mstep_aggregate)
         if prec == E.PREC_MIXED and args.counts_round:
             p.set_option(E.Plan.OPT_COUNTS_ROUND, 1)
+        p.set_option(E.Plan.OPT_ESTEP_PAIR, args.estep_pair)
         p.bind(images, mask, x, y, z, rot, w)
         return p
 
@@ -569,7 +572,8 @@ def finish(args, prob, workspace, ctx, ws, rank, precision, value, ms_step, st, 
     p_eff = int(prob.mask.sum())
     if args.diff == "poisson":
         flops = 8.0 * p_eff * pairs  # 4 GEMM-equivalents (num, den, B, C) x 2 FLOP
-        kernel = "tc_estep_kernel" if precision == "mixed" else "estep_fp32_kernel"
+        kernel = ("tc_estep_pair_kernel" if args.estep_pair else "tc_estep_kernel") \
+            if precision == "mixed" else "estep_fp32_kernel"
     else:
         flops = 2.0 * p_eff * pairs  # one GEMM-equivalent (counts x log slice) x 2 FLOP
         kernel = "tc_estep_pois_kernel" if precision == "mixed" else "estep_pois_fp32_kernel"
@@ -605,6 +609,8 @@ def finish(args, prob, workspace, ctx, ws, rank, precision, value, ms_step, st, 
                                      2: "G hi, H hi+lo", 1: "G hi+lo, H hi",
                                      0: "G, H fp16 hi"}[args.estep_ghlo],
                            mstep_atomics="warp-aggregated" if args.mstep_aggregate else "per pair",
+                           estep_kernel="CTA pairs (256-row MMAs)" if args.estep_pair
+                           else "single CTAs",
                            counts="counts above 2048 rounded to fp16" if
                            (args.counts_round and precision == "mixed") else "exact"),
             "iter_per_s": ws * 1e3 / ms_step,

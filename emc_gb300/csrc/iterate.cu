@@ -1459,6 +1459,11 @@ extern "C" int emc_plan_set_option(emc_plan* p, int option, int value) {
     p->estep_raster = value;
     return EMC_OK;
   }
+  if (option == EMC_OPT_ESTEP_PAIR) {
+    EMC_REQUIRE(ctx, value == 0 || value == 1, "plan_set_option: pair %d", value);
+    p->estep_pair = value;
+    return EMC_OK;
+  }
   if (option == EMC_OPT_MSTEP_AGGREGATE) {
     EMC_REQUIRE(ctx, value == 0 || value == 1, "plan_set_option: aggregate %d", value);
     p->mstep_aggregate = value;

@@ -99,6 +99,7 @@ struct emc_plan {
   int estep_gh_lo = -1;   // tensor E-step lo terms: bit 0 G, bit 1 H; -1 auto
   int mstep_q_lo = 0;     // tensor M-step: Q as FP16 hi + lo (1) or hi only (0)
   int estep_raster = 8;     // tensor E-step tile order (EMC_OPT_ESTEP_RASTER)
+  int estep_pair = 1;       // full scans on CTA pairs (EMC_OPT_ESTEP_PAIR)
   int mstep_aggregate = 0;  // tensor M-step: warp-aggregated float atomics (nearest)
 
   std::vector<void*> allocs;

@@ -261,6 +261,85 @@ struct TcEstepArgs {
   int* status;
 };
 
+// Epilogue of the likelihood kernels (warps 2 .. 2 + EPI_WARPS - 1): EPI_PARTS
+// warps per TMEM lane quarter, each on a part of the 128 columns, so that
+// the expf / divide latency of one hides behind another.  Reads B, den, C and
+// num of this CTA's 128 patterns x 128 rotations from TMEM, writes L and
+// phi and the tile's (max, sum exp) per pattern.
+__device__ __forceinline__ void estep_epilogue(const TcEstepArgs& a, uint32_t tmem, uint64_t* accum,
+                                               const float* s_A, const float* s_scale,
+                                               const float* s_lw, float2* s_half, int warp,
+                                               int lane, int n0, int r0, int rt) {
+  using namespace es;
+  // EPI_PARTS warps per TMEM lane quarter, each on a part of the 128
+  // columns, so that the expf / divide latency of one hides behind another
+  const int quarter = warp & 3;  // TMEM lanes this warp may access
+  const int half = (warp - 2) >> 2;  // column part
+  const int row = quarter * 32 + lane;
+  const int n = n0 + row;
+  const bool nok = n < a.N;
+  const float ci = nok ? a.cnorm[n] : 1.0f;
+  float m = -INFINITY, ssum = 0.0f;
+  int nbad = 0;
+  if (ptx::mbar_wait_sleep(accum, 0, a.status, 2, 256)) {
+    ptx::tc_fence_after();
+    const uint32_t lane_addr = tmem + ((uint32_t)(quarter * 32) << 16);
+    for (int c0 = half * (BN / EPI_PARTS); c0 < (half + 1) * (BN / EPI_PARTS); c0 += 16) {
+      float vn[16], vd[16], vb[16], vc[16];
+      ptx::tmem_ld16(lane_addr + 0 + c0, vb);
+      ptx::tmem_ld16(lane_addr + 128 + c0, vd);
+      ptx::tmem_ld16(lane_addr + 256 + c0, vc);
+      ptx::tmem_ld16(lane_addr + 384 + c0, vn);
+      ptx::tmem_wait_ld();
+#pragma unroll
+      for (int j = 0; j < 16; ++j) {
+        const int cl = c0 + j;
+        const int r = r0 + cl;
+        const float num = vn[j] * a.k2_inv, den = vd[j] * 256.0f;
+        const float B = vb[j], Cc = vc[j] * a.k2_inv;
+        const float sc = s_scale[cl];
+        bool ok = nok && r < a.R && sc > 0.0f;
+        float iphi = 1.0f, phi = 1.0f;
+        if (!a.known_intensity) {
+          ok = ok && num > 0.0f && den > 0.0f;
+          iphi = den / num;
+          phi = ci * num / den;
+        }
+        const float Sig = s_A[cl] - 2.0f * B * iphi + Cc * iphi * iphi;
+        const float L = ok ? s_lw[cl] - Sig * sc : -INFINITY;
+        if (nok && r < a.R) {
+          if (!ok) nbad++;
+          a.L[(size_t)r * a.N + n] = L;
+          a.PHI[(size_t)r * a.N + n] = ok ? phi : 1.0f;
+        }
+        if (L > m) {
+          ssum = ssum * expf(m - L) + 1.0f;
+          m = L;
+        } else if (L > -INFINITY) {
+          ssum += expf(L - m);
+        }
+      }
+    }
+  }
+  // combine the parts' (max, sum exp) of each row
+  if (half > 0) s_half[(half - 1) * BM + row] = make_float2(m, ssum);
+  asm volatile("bar.sync 1, %0;" ::"n"(EPI_WARPS * 32) : "memory");  // epilogue warps only
+  if (half == 0) {
+    float M = m;
+    for (int q = 1; q < EPI_PARTS; ++q) M = fmaxf(M, s_half[(q - 1) * BM + row].x);
+    float S = 0.0f;
+    if (M > -INFINITY) {
+      S = ssum * expf(m - M);
+      for (int q = 1; q < EPI_PARTS; ++q) {
+        const float2 o = s_half[(q - 1) * BM + row];
+        S += o.y * expf(o.x - M);
+      }
+    }
+    if (nok) a.part[(size_t)rt * a.N + n] = make_float2(M, S);
+  }
+  if (nbad) atomicAdd(a.bad, nbad);
+}
+
 __global__ void __launch_bounds__(es::THREADS, 1)
     tc_estep_kernel(const __grid_constant__ CUtensorMap mK, const __grid_constant__ CUtensorMap mK2h,
                     const __grid_constant__ CUtensorMap mK2l, const __grid_constant__ CUtensorMap mMp,
@@ -368,80 +447,162 @@ __global__ void __launch_bounds__(es::THREADS, 1)
       ptx::mma_commit(accum);
     }
   } else {
-    // ------------------------------------------------ epilogue (warps 2-9)
-    // EPI_PARTS warps per TMEM lane quarter, each on a part of the 128
-    // columns, so that the expf / divide latency of one hides behind another
-    const int quarter = warp & 3;  // TMEM lanes this warp may access
-    const int half = (warp - 2) >> 2;  // column part
-    const int row = quarter * 32 + lane;
-    const int n = n0 + row;
-    const bool nok = n < a.N;
-    const float ci = nok ? a.cnorm[n] : 1.0f;
-    float m = -INFINITY, ssum = 0.0f;
-    int nbad = 0;
-    if (ptx::mbar_wait(accum, 0, a.status, 2)) {
-      ptx::tc_fence_after();
-      const uint32_t lane_addr = tmem + ((uint32_t)(quarter * 32) << 16);
-      for (int c0 = half * (BN / EPI_PARTS); c0 < (half + 1) * (BN / EPI_PARTS); c0 += 16) {
-        float vn[16], vd[16], vb[16], vc[16];
-        ptx::tmem_ld16(lane_addr + 0 + c0, vb);
-        ptx::tmem_ld16(lane_addr + 128 + c0, vd);
-        ptx::tmem_ld16(lane_addr + 256 + c0, vc);
-        ptx::tmem_ld16(lane_addr + 384 + c0, vn);
-        ptx::tmem_wait_ld();
-#pragma unroll
-        for (int j = 0; j < 16; ++j) {
-          const int cl = c0 + j;
-          const int r = r0 + cl;
-          const float num = vn[j] * a.k2_inv, den = vd[j] * 256.0f;
-          const float B = vb[j], Cc = vc[j] * a.k2_inv;
-          const float sc = s_scale[cl];
-          bool ok = nok && r < a.R && sc > 0.0f;
-          float iphi = 1.0f, phi = 1.0f;
-          if (!a.known_intensity) {
-            ok = ok && num > 0.0f && den > 0.0f;
-            iphi = den / num;
-            phi = ci * num / den;
-          }
-          const float Sig = s_A[cl] - 2.0f * B * iphi + Cc * iphi * iphi;
-          const float L = ok ? s_lw[cl] - Sig * sc : -INFINITY;
-          if (nok && r < a.R) {
-            if (!ok) nbad++;
-            a.L[(size_t)r * a.N + n] = L;
-            a.PHI[(size_t)r * a.N + n] = ok ? phi : 1.0f;
-          }
-          if (L > m) {
-            ssum = ssum * expf(m - L) + 1.0f;
-            m = L;
-          } else if (L > -INFINITY) {
-            ssum += expf(L - m);
-          }
-        }
-      }
-    }
-    // combine the parts' (max, sum exp) of each row
-    if (half > 0) s_half[(half - 1) * BM + row] = make_float2(m, ssum);
-    asm volatile("bar.sync 1, %0;" ::"n"(EPI_WARPS * 32) : "memory");  // epilogue warps only
-    if (half == 0) {
-      float M = m;
-      for (int q = 1; q < EPI_PARTS; ++q) M = fmaxf(M, s_half[(q - 1) * BM + row].x);
-      float S = 0.0f;
-      if (M > -INFINITY) {
-        S = ssum * expf(m - M);
-        for (int q = 1; q < EPI_PARTS; ++q) {
-          const float2 o = s_half[(q - 1) * BM + row];
-          S += o.y * expf(o.x - M);
-        }
-      }
-      if (nok) a.part[(size_t)rt * a.N + n] = make_float2(M, S);
-    }
-    if (nbad) atomicAdd(a.bad, nbad);
+    // ------------------------------------------------ epilogue (warps 2-17)
+    estep_epilogue(a, tmem, accum, s_A, s_scale, s_lw, s_half, warp, lane, n0, r0, rt);
   }
   ptx::tc_fence_before();
   __syncthreads();
   if (warp == 1) {
     ptx::tc_fence_after();
     ptx::tmem_dealloc(tmem, 512);
+  }
+}
+
+// ------------------------------------------------ E-step on CTA pairs -----
+// The same contractions over 256 patterns x 128 rotations per cluster of two
+// CTAs, with 256-row MMAs (cta_group::2) issued by rank 0.  Each CTA keeps
+// its own 128 patterns' tiles (K, K^2 hi, K^2 lo) and one half of every
+// rotation-side operand: rank 0 the G and H columns of the [G | M'S] and
+// [H | M'] pairs, rank 1 the M'S and M' columns, and 64 of the 128 G lo rows
+// each.  Per 32-pixel stage a CTA loads 36 KB (44 KB with K^2 lo) instead of
+// 56-64 KB for the same MMA work, and five stages fit in shared memory: the
+// loads in flight cover more of the L2 / HBM latency that stalls the MMAs.  Both CTAs' loads complete
+// on rank 0's `full` barriers; rank 0's commits arrive on both CTAs' `empty`
+// and `accum` barriers.  The epilogue is the single-CTA kernel's, per CTA.
+namespace es2 {
+constexpr int STAGES = 5;
+constexpr int TILE = 128 * es::BK * 2;  // 8 KB: 128 rows of one operand
+constexpr int HALF = TILE / 2;          // 64 rows (G lo half)
+constexpr int oK = 0, oK2h = TILE, oK2l = 2 * TILE, oB1 = 3 * TILE, oB2 = 4 * TILE,
+              oGl = 5 * TILE;
+constexpr int STAGE_BYTES = 5 * TILE + HALF;  // 44 KB; no H lo (known intensity runs single CTAs)
+// barriers (256 B), per-rotation rows (3 x 128 floats), epilogue parts
+constexpr int EXTRA = 256 + 3 * es::BN * 4 + (es::EPI_PARTS - 1) * es::BM * 8;
+constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + EXTRA + 1024;
+static_assert(SMEM_BYTES <= 232448, "shared memory of the pair kernel");
+}  // namespace es2
+
+__global__ void __launch_bounds__(es::THREADS, 1)
+    tc_estep_pair_kernel(const __grid_constant__ CUtensorMap mK,
+                         const __grid_constant__ CUtensorMap mK2h,
+                         const __grid_constant__ CUtensorMap mK2l,
+                         const __grid_constant__ CUtensorMap mMp,
+                         const __grid_constant__ CUtensorMap mMS,
+                         const __grid_constant__ CUtensorMap mGh,
+                         const __grid_constant__ CUtensorMap mGl64,
+                         const __grid_constant__ CUtensorMap mHh, TcEstepArgs a) {
+  using namespace es;
+  using es2::STAGES;
+  using es2::STAGE_BYTES;
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint64_t* full = (uint64_t*)(smem + STAGES * STAGE_BYTES);
+  uint64_t* empty = full + STAGES;
+  uint64_t* accum = empty + STAGES;
+  uint32_t* tmem_slot = (uint32_t*)(accum + 1);
+  float* s_A = (float*)(smem + STAGES * STAGE_BYTES + 256);
+  float* s_scale = s_A + BN;
+  float* s_lw = s_scale + BN;
+  float2* s_half = (float2*)(s_lw + BN);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t rank = ptx::cluster_ctarank();
+  const float sg = *a.sigma;
+  const float inv2s2 = 1.0f / (2.0f * sg * sg);
+  const int n_ptp = (a.n_pt + 1) / 2;
+  int ptp, rt;
+  raster_tile((int)(blockIdx.x >> 1) + a.tile0, a.raster, n_ptp, a.n_rt, ptp, rt);
+  const int pt = 2 * ptp + (int)rank;  // may be n_pt (no patterns) when n_pt is odd
+  const int n0 = pt * BM, r0 = rt * BN;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      ptx::mbar_init(&full[s], 1);
+      ptx::mbar_init(&empty[s], 1);
+    }
+    ptx::mbar_init(accum, 1);
+    ptx::fence_mbar_init();
+  }
+  if (threadIdx.x < BN) {
+    const int r = r0 + threadIdx.x;
+    const float cnt = r < a.R ? a.rot_cnt[r] : 0.0f;
+    s_A[threadIdx.x] = r < a.R ? a.rot_A[r] : 0.0f;
+    s_scale[threadIdx.x] = cnt > 0.0f ? inv2s2 / cnt : -1.0f;
+    s_lw[threadIdx.x] = r < a.R ? logf(a.rotw[r]) : 0.0f;
+  }
+  if (warp == 1) {
+    ptx::tmem_alloc_pair(tmem_slot, 512);
+    ptx::tmem_relinquish_pair();
+  }
+  ptx::tc_fence_before();
+  __syncthreads();
+  ptx::cluster_sync();  // both CTAs' barriers initialised and TMEM allocated
+  ptx::tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+  // the K^2 lo MMA runs for a k-block when either pattern tile needs it
+  const int pt0 = 2 * ptp, pt1 = 2 * ptp + 1;
+  const unsigned char* flags0 = a.k2lo_any + (size_t)pt0 * a.nkb;
+  const unsigned char* flags1 = pt1 < a.n_pt ? a.k2lo_any + (size_t)pt1 * a.nkb : nullptr;
+  const bool glo = (a.gh_lo & 1) != 0;  // H lo (gh_lo bit 1) runs on single CTAs
+
+  if (warp == 0) {
+    // ------------------------------------------------ TMA producer (both CTAs)
+    if (lane == 0) {
+      const CUtensorMap* mb1 = rank ? &mMS : &mGh;
+      const CUtensorMap* mb2 = rank ? &mMp : &mHh;
+      for (int kb = 0; kb < a.nkb; ++kb) {
+        const int s = kb % STAGES;
+        const uint32_t ph = (kb / STAGES) & 1;
+        if (!ptx::mbar_wait(&empty[s], ph ^ 1, a.status, 0)) break;
+        const bool lo = flags0[kb] != 0 || (flags1 && flags1[kb] != 0);
+        const uint32_t bytes = (lo ? 5 : 4) * es2::TILE + (glo ? es2::HALF : 0);
+        if (rank == 0) ptx::mbar_arrive_expect_tx(&full[s], 2 * bytes);  // both CTAs' loads
+        const uint32_t fb = ptx::mapa_shared(ptx::smem_u32(&full[s]), 0);
+        unsigned char* st = smem + s * STAGE_BYTES;
+        const int x = kb * BK;
+        ptx::tma_load_2d_pair(st + es2::oK, &mK, x, n0, fb);
+        ptx::tma_load_2d_pair(st + es2::oK2h, &mK2h, x, n0, fb);
+        if (lo) ptx::tma_load_2d_pair(st + es2::oK2l, &mK2l, x, n0, fb);
+        ptx::tma_load_2d_pair(st + es2::oB1, mb1, x, r0, fb);
+        ptx::tma_load_2d_pair(st + es2::oB2, mb2, x, r0, fb);
+        if (glo) ptx::tma_load_2d_pair(st + es2::oGl, &mGl64, x, r0 + 64 * (int)rank, fb);
+      }
+    }
+  } else if (warp == 1) {
+    // ------------------------------------------------ MMA issuer (rank 0)
+    if (rank == 0 && lane == 0) {
+      constexpr uint32_t idesc2 = ptx::idesc_f16(2 * BM, 2 * BN);  // 256 x 256 pairs
+      constexpr uint32_t idesc1 = ptx::idesc_f16(2 * BM, BN);      // 256 x 128 lo terms
+      for (int kb = 0; kb < a.nkb; ++kb) {
+        const int s = kb % STAGES;
+        const uint32_t ph = (kb / STAGES) & 1;
+        if (!ptx::mbar_wait(&full[s], ph, a.status, 1)) break;
+        ptx::tc_fence_after();
+        const bool lo = flags0[kb] != 0 || (flags1 && flags1[kb] != 0);
+        const uint32_t base = ptx::smem_u32(smem + s * STAGE_BYTES);
+#pragma unroll
+        for (int ks = 0; ks < BK / 16; ++ks) {
+          auto d = [&](int off) { return ptx::smem_desc(base + off + ks * 32, 512, 4); };
+          const uint32_t acc = (kb | ks) ? 1u : 0u;
+          ptx::mma_f16_pair(tmem + 0, d(es2::oK), d(es2::oB1), idesc2, acc);      // B hi | den
+          ptx::mma_f16_pair(tmem + 256, d(es2::oK2h), d(es2::oB2), idesc2, acc);  // C hi | num
+          if (glo) ptx::mma_f16_pair(tmem + 0, d(es2::oK), d(es2::oGl), idesc1, 1u);
+          if (lo) ptx::mma_f16_pair(tmem + 256, d(es2::oK2l), d(es2::oB2), idesc2, 1u);
+        }
+        ptx::mma_commit_pair(&empty[s], 0x3);
+      }
+      ptx::mma_commit_pair(accum, 0x3);
+    }
+  } else {
+    // ------------------------------------------------ epilogue (warps 2-17)
+    estep_epilogue(a, tmem, accum, s_A, s_scale, s_lw, s_half, warp, lane, n0, r0, rt);
+  }
+  ptx::tc_fence_before();
+  __syncthreads();
+  ptx::cluster_sync();  // the pair's MMAs and barrier traffic are over in both CTAs
+  if (warp == 1) {
+    ptx::tc_fence_after();
+    ptx::tmem_dealloc_pair(tmem, 512);
   }
 }
 
@@ -573,7 +734,7 @@ __global__ void __launch_bounds__(ep::THREADS, 1)
     const bool nok = n < a.N;
     const float ci = nok ? a.cnorm[n] : 1.0f;
     const float Ki = nok ? a.Ksum[n] : 0.0f;
-    const bool waited = ptx::mbar_wait(accum, 0, a.status, 10);
+    const bool waited = ptx::mbar_wait_sleep(accum, 0, a.status, 10, 256);
     if (waited) ptx::tc_fence_after();
     const uint32_t lane_addr = tmem + ((uint32_t)(quarter * 32) << 16);
     {
@@ -868,7 +1029,7 @@ __global__ void __launch_bounds__(ms::THREADS, 1)
       const bool live = rok && Tr > 1e-10f;
       RotMat Rm = {};
       if (rok) Rm = quat_to_matrix(a.rot + 4 * (size_t)r);
-      if (!ptx::mbar_wait(&tfull[b], (j >> 1) & 1, a.status, 6)) break;
+      if (!ptx::mbar_wait_sleep(&tfull[b], (j >> 1) & 1, a.status, 6, 128)) break;
       ptx::tc_fence_after();
       const uint32_t lane_addr = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(b * BN);
       for (int c0 = half * 128; c0 < half * 128 + 128; c0 += 16) {
@@ -905,6 +1066,7 @@ __global__ void __launch_bounds__(ms::THREADS, 1)
 struct TcState {
   CUtensorMap mK, mK2h, mK2l, mQh, mQl, mKt;
   CUtensorMap rot[6];    // M', MS, Gh, Gl, Hh, Hl: 128-row boxes
+  CUtensorMap gl64;        // G lo: 64-row boxes (CTA-pair halves)
   CUtensorMap mLh, mLl;  // true Poisson: log-slices hi / lo (in Gh, Gl), 256-row boxes
   __half *Mp, *MSh, *Gh, *Gl, *Hh, *Hl;
   int* status;
@@ -962,12 +1124,16 @@ int tc_bind(emc_plan* p) {
       if (!rc) rc = make_map(ctx, &st->mK2l, p->K2lo, Np, Kp, 128, 32);
       const __half* ro[6] = {st->Mp, st->MSh, st->Gh, st->Gl, st->Hh, st->Hl};
       for (int j = 0; j < 6 && !rc; ++j) rc = make_map(ctx, &st->rot[j], ro[j], Rp, Kp, 128, 32);
+      if (!rc) rc = make_map(ctx, &st->gl64, st->Gl, Rp, Kp, 64, 32);
     }
     if (!rc) rc = make_map(ctx, &st->mQh, p->Qh, Rp, Np, 128, 64);
     if (!rc) rc = make_map(ctx, &st->mKt, p->KhT, Kp, Np, 256, 64);
     if (rc) return rc;
     EMC_CUDA(ctx, cudaFuncSetAttribute(tc_estep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        es::SMEM_BYTES));
+    EMC_CUDA(ctx, cudaFuncSetAttribute(tc_estep_pair_kernel,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       es2::SMEM_BYTES));
     EMC_CUDA(ctx, cudaFuncSetAttribute(tc_estep_pois_kernel,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, ep::SMEM_BYTES));
     EMC_CUDA(ctx, cudaFuncSetAttribute(tc_mstep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1088,6 +1254,30 @@ static int estep_launch(emc_plan* p, int raster, int first, int count, bool full
   a.bad = p->flags + 4;
   a.status = st->status;
   const CUtensorMap* rm = st->rot;
+  if (p->estep_pair && !a.tiles && !(a.gh_lo & 2)) {
+    // CTA pairs: tiles are (pattern-tile pair, rotation tile)
+    const int total = ((a.n_pt + 1) / 2) * a.n_rt;
+    first = std::max(0, std::min(first, total));
+    const int pairs = std::min(total - first, count);
+    a.tile0 = first;
+    if (pairs == 0) return EMC_OK;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(2 * pairs);
+    cfg.blockDim = dim3(es::THREADS);
+    cfg.dynamicSmemBytes = es2::SMEM_BYTES;
+    cfg.stream = ctx->stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = 2;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    const cudaError_t e = cudaLaunchKernelEx(&cfg, tc_estep_pair_kernel, st->mK, st->mK2h, st->mK2l,
+                                             rm[0], rm[1], rm[2], st->gl64, rm[4], a);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "tc_estep_pair_kernel launch");
+    return after_launch(ctx, "tc_estep_pair_kernel");
+  }
   const int total = a.n_pt * a.n_rt;
   first = a.tiles ? 0 : std::max(0, std::min(first, total));
   const int grid = a.tiles ? p->prune_n_tiles : std::min(total - first, count);
@@ -1104,6 +1294,18 @@ int tc_estep(emc_plan* p) {
   int rc = estep_operands(p);
   if (rc) return rc;
   return estep_launch(p, p->estep_raster, 0, INT_MAX, false);
+}
+
+// The likelihood lo terms in force: bit 0 G lo, bit 1 H lo (auto: H lo when
+// the intensity is known).
+static int estep_gh_lo(const emc_plan* p) {
+  return p->estep_gh_lo >= 0 ? p->estep_gh_lo : (p->d.known_intensity ? 3 : 1);
+}
+
+// Full scans of the reference likelihood run on CTA pairs unless switched
+// off or H lo is needed (the pair kernel has no H lo slot).
+static bool estep_uses_pair(const emc_plan* p) {
+  return p->estep_pair && p->d.diff != EMC_DIFF_TRUE_POISSON && !(estep_gh_lo(p) & 2);
 }
 
 // One timed launch of the likelihood kernel over tiles [first, first + count)
@@ -1126,10 +1328,12 @@ int tc_time_estep(emc_plan* p, int raster, int first, int count, float* ms) {
   return rc;
 }
 
+// Units of the full likelihood grid as estep_launch counts them: tiles, or
+// CTA-pair tiles for the pair kernel.
 int tc_estep_tiles(emc_plan* p) {
   const int n_pt = p->Np / 128;
-  const int n_rt = p->d.diff == EMC_DIFF_TRUE_POISSON ? ceil_div(p->Rp, ep::BN) : p->Rp / es::BN;
-  return n_pt * n_rt;
+  if (p->d.diff == EMC_DIFF_TRUE_POISSON) return n_pt * ceil_div(p->Rp, ep::BN);
+  return (estep_uses_pair(p) ? (n_pt + 1) / 2 : n_pt) * (p->Rp / es::BN);
 }
 
 // Raster autotuner.  The likelihood kernel streams two operand panels per
@@ -1151,10 +1355,11 @@ int tc_autotune(emc_plan* p, int waves, int* best, float* best_ms) {
   int rc = estep_operands(p);
   if (rc) return rc;
   const bool pois = p->d.diff == EMC_DIFF_TRUE_POISSON;
-  const int n_pt = p->Np / 128;
+  const bool pair = !pois && estep_uses_pair(p);
+  const int n_pt = pair ? (p->Np / 128 + 1) / 2 : p->Np / 128;
   const int n_rt = pois ? ceil_div(p->Rp, ep::BN) : p->Rp / es::BN;
   const int total = n_pt * n_rt;
-  const int count = std::min(total, std::max(1, waves) * ctx->sm_count);
+  const int count = std::min(total, std::max(1, waves) * (pair ? ctx->sm_count / 2 : ctx->sm_count));
   std::vector<int> firsts;
   if (count >= total) {
     firsts.push_back(0);

@@ -51,6 +51,8 @@ CONFIGS = {
     "lowcount": Config("lowcount", 128, 3000, 1.5, 28, 50000, 80, (0.2, 2.0), 6, 6, 30,
                        masked_fraction=0.5),
     "large": Config("large", 256, 20000, 1.5, 56, 100000, 10000, (0.5, 1.5), 12, 12, 5),
+    # the mid geometry with a fifth of the patterns: kernel profiles of a few GB
+    "mid_small": Config("mid_small", 128, 3000, 1.5, 28, 4000, 5000, (0.5, 1.5), 6, 8, 1),
 }
 
 

@@ -449,6 +449,12 @@ int emc_batch_destroy(emc_batch* batch);
  * running through all rotation tiles.  |g| <= 4096.  Results do not depend on
  * it; L2 reuse of the operand panels does. */
 #define EMC_OPT_ESTEP_RASTER 6
+/* EMC_OPT_ESTEP_PAIR: 1 (default) runs full scans of the reference
+ * likelihood on clusters of two CTAs with 256-row MMAs (each CTA stores half
+ * of the rotation-side operands, which cuts the shared-memory traffic that
+ * bounds the single-CTA kernel); 0 runs every scan on single CTAs.  Pruned
+ * iterations always use single CTAs.  Results are the same either way. */
+#define EMC_OPT_ESTEP_PAIR 7
 int emc_plan_set_option(emc_plan* plan, int option, int value);
 /* Tile-order autotuner of the tensor-core likelihood kernel: expands d_model
  * (sigma as in emc_iterate), times the kernel for each candidate

@@ -105,11 +105,11 @@ def profile_traffic(kernel_key):
     d = os.path.join(ROOT, "profiles")
     if not os.path.isdir(d):
         return None
-    for name in sorted(os.listdir(d)):
-        if name.startswith(kernel_key) and name.endswith(".md"):
-            m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", open(os.path.join(d, name)).read())
-            if m:
-                return float(m.group(1))
+    path = os.path.join(d, kernel_key + ".md")
+    if os.path.exists(path):
+        m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", open(path).read())
+        if m:
+            return float(m.group(1))
     return None
 
 

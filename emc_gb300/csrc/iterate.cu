@@ -82,30 +82,41 @@ __global__ void pattern_norm_kernel(const float* __restrict__ images, const int*
 }
 
 // Compacted pattern operands.  flags[0] bit 0: non-finite input; bit 1: a
-// count outside [0, 2048] or not an integer (no exact FP16 form).
+// count that is not an integer in [0, 65504] (no FP16 form); bit 3: an
+// integer count above 2048 (FP16 rounds it); flags[8]: the largest integer
+// count.  One block per (pattern, 256 compacted pixels), pixel blocks the
+// fast index so that a pattern's row stays in L2 while its blocks run; flags
+// reduced per warp before one atomic.
 __global__ void pattern_ops_kernel(const float* __restrict__ images, const int* __restrict__ pix,
                                    const float* __restrict__ cnorm, int n2, int N, int Kp,
                                    float* __restrict__ Kraw, float* __restrict__ Kt,
                                    float* __restrict__ K2, int* __restrict__ flags,
                                    const int* __restrict__ perm) {
-  const int i = blockIdx.x;  // patterns on x: N may exceed the 65,535 of y
-  const int q = blockIdx.y * blockDim.x + threadIdx.x;
-  if (q >= Kp) return;
-  const int p = pix[q];
+  const int nqb = (Kp + 255) / 256;
+  const int i = (int)(blockIdx.x / nqb);
+  const int q = (int)(blockIdx.x % nqb) * 256 + threadIdx.x;
+  const bool in = q < Kp;
+  const int p = in ? pix[q] : -1;
   float k = 0.0f;
+  int bits = 0, vmax = 0;
   if (p >= 0) {
     const float v = __ldg(images + (size_t)(perm ? perm[i] : i) * n2 + p);
-    if (!isfinite(v)) atomicOr(flags, 1);
-    // bit 1: not an integer in [0, 65504] (no FP16 form); bit 3: an integer
-    // above 2048 (FP16 rounds it); flags[8]: the largest integer count
+    if (!isfinite(v)) bits |= 1;
     if (!(v >= 0.0f && v <= 65504.0f && v == rintf(v))) {
-      atomicOr(flags, 2);
+      bits |= 2;
     } else {
-      if (v > 2048.0f) atomicOr(flags, 8);
-      atomicMax(flags + 8, (int)v);
+      if (v > 2048.0f) bits |= 8;
+      vmax = (int)v;
     }
     k = __fmul_rn(v, __ldg(cnorm + i));
   }
+  bits = __reduce_or_sync(0xffffffffu, (unsigned)bits);
+  vmax = __reduce_max_sync(0xffffffffu, vmax);
+  if ((threadIdx.x & 31) == 0) {
+    if (bits) atomicOr(flags, bits);
+    if (vmax) atomicMax(flags + 8, vmax);
+  }
+  if (!in) return;
   const size_t o = (size_t)i * Kp + q;
   Kraw[o] = k;
   const float kt = k >= 1e-10f ? k : 0.0f;  // the reference's (double)k > 1e-10
@@ -988,7 +999,7 @@ int emc::pattern_side(emc_plan* p, const int* d_perm, bool with_tc) {
       p->images, p->mask, n2, N, p->d.normalize_images, p->cnorm, d_perm);
   if ((rc = after_launch(ctx, "pattern_norm_kernel"))) return rc;
   // Kt / K2 exist only for the FP32 path (null: not written).
-  pattern_ops_kernel<<<dim3(N, ceil_div(p->Kp, 256)), 256, 0, ctx->stream>>>(
+  pattern_ops_kernel<<<(unsigned)N * (unsigned)ceil_div(p->Kp, 256), 256, 0, ctx->stream>>>(
       p->images, p->pix, p->cnorm, n2, N, p->Kp, p->Kraw, p->Kt, p->K2, p->flags, d_perm);
   if ((rc = after_launch(ctx, "pattern_ops_kernel"))) return rc;
   row_sum_kernel<<<N, 256, 0, ctx->stream>>>(p->Kraw, p->Kp, p->Kp, p->Ksum);

@@ -28,6 +28,8 @@
 #include <cstring>
 #include <vector>
 
+#include <cuda_fp16.h>
+
 #include "geometry.cuh"
 #include "kernels.cuh"
 #include "plan.cuh"
@@ -86,21 +88,27 @@ __global__ void pattern_norm_kernel(const float* __restrict__ images, const int*
 // integer count above 2048 (FP16 rounds it); flags[8]: the largest integer
 // count.  One block per (pattern, 256 compacted pixels), pixel blocks the
 // fast index so that a pattern's row stays in L2 while its blocks run; flags
-// reduced per warp before one atomic.
+// and part[i][block] (the block's sum of k, FP64, fixed order) reduced by
+// warp shuffles and one barrier.  Kraw / Kt / K2 (FP32 path) may be null;
+// with Kh non-null the kernel also writes the tensor path's FP16 operands
+// (the same values as tc_pattern_ops_kernel with scale k2_scale).
 __global__ void pattern_ops_kernel(const float* __restrict__ images, const int* __restrict__ pix,
                                    const float* __restrict__ cnorm, int n2, int N, int Kp,
                                    float* __restrict__ Kraw, float* __restrict__ Kt,
                                    float* __restrict__ K2, int* __restrict__ flags,
-                                   const int* __restrict__ perm) {
+                                   const int* __restrict__ perm, double* __restrict__ part,
+                                   __half* __restrict__ Kh, __half* __restrict__ K2h,
+                                   __half* __restrict__ K2l, float k2_scale) {
   const int nqb = (Kp + 255) / 256;
   const int i = (int)(blockIdx.x / nqb);
   const int q = (int)(blockIdx.x % nqb) * 256 + threadIdx.x;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const bool in = q < Kp;
   const int p = in ? pix[q] : -1;
-  float k = 0.0f;
+  float v = 0.0f, k = 0.0f;
   int bits = 0, vmax = 0;
   if (p >= 0) {
-    const float v = __ldg(images + (size_t)(perm ? perm[i] : i) * n2 + p);
+    v = __ldg(images + (size_t)(perm ? perm[i] : i) * n2 + p);
     if (!isfinite(v)) bits |= 1;
     if (!(v >= 0.0f && v <= 65504.0f && v == rintf(v))) {
       bits |= 2;
@@ -110,33 +118,59 @@ __global__ void pattern_ops_kernel(const float* __restrict__ images, const int* 
     }
     k = __fmul_rn(v, __ldg(cnorm + i));
   }
+  double sum = (double)k;
+  for (int o = 16; o > 0; o >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, o);
   bits = __reduce_or_sync(0xffffffffu, (unsigned)bits);
   vmax = __reduce_max_sync(0xffffffffu, vmax);
-  if ((threadIdx.x & 31) == 0) {
-    if (bits) atomicOr(flags, bits);
-    if (vmax) atomicMax(flags + 8, vmax);
+  __shared__ double wsum[8];
+  __shared__ int wbits[8], wmax[8];
+  if (lane == 0) {
+    wsum[warp] = sum;
+    wbits[warp] = bits;
+    wmax[warp] = vmax;
   }
-  if (!in) return;
-  const size_t o = (size_t)i * Kp + q;
-  Kraw[o] = k;
-  const float kt = k >= 1e-10f ? k : 0.0f;  // the reference's (double)k > 1e-10
-  if (Kt) Kt[o] = kt;
-  if (K2) K2[o] = __fmul_rn(kt, kt);
+  if (in) {
+    const size_t o = (size_t)i * Kp + q;
+    if (Kraw) Kraw[o] = k;
+    const float kt = k >= 1e-10f ? k : 0.0f;  // the reference's (double)k > 1e-10
+    if (Kt) Kt[o] = kt;
+    if (K2) K2[o] = __fmul_rn(kt, kt);
+    if (Kh) {
+      const __half kh = __float2half_rn(v);
+      const float kr = __half2float(kh);
+      const float k2 = kr * kr * k2_scale;
+      const __half hi = __float2half_rn(k2);
+      Kh[o] = kh;
+      if (K2h) {
+        K2h[o] = hi;
+        K2l[o] = __float2half_rn(k2 - __half2float(hi));
+      }
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    int b = 0, m = 0;
+    for (int j = 0; j < 8; ++j) {
+      t += wsum[j];
+      b |= wbits[j];
+      m = max(m, wmax[j]);
+    }
+    part[blockIdx.x] = t;
+    if (b) atomicOr(flags, b);
+    // the maximum settles early: skip the atomic when this block cannot raise it
+    if (m > flags[8]) atomicMax(flags + 8, m);
+  }
 }
 
-__global__ void row_sum_kernel(const float* __restrict__ a, int ncol, int ld,
-                               float* __restrict__ out) {
-  const int r = blockIdx.x;
+// Ksum[i] = the sum of pattern i's block partials (in block order).
+__global__ void pattern_sums_kernel(const double* __restrict__ part, int N, int nqb,
+                                    float* __restrict__ Ksum) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
   double s = 0.0;
-  for (int c = threadIdx.x; c < ncol; c += blockDim.x) s += (double)a[(size_t)r * ld + c];
-  __shared__ double sh[256];
-  sh[threadIdx.x] = s;
-  __syncthreads();
-  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-    if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) out[r] = (float)sh[0];
+  for (int b = 0; b < nqb; ++b) s += part[(size_t)i * nqb + b];
+  Ksum[i] = (float)s;
 }
 
 // ------------------------------------------------------------ expand -----
@@ -999,12 +1033,20 @@ int emc::pattern_side(emc_plan* p, const int* d_perm, bool with_tc) {
       p->images, p->mask, n2, N, p->d.normalize_images, p->cnorm, d_perm);
   if ((rc = after_launch(ctx, "pattern_norm_kernel"))) return rc;
   // Kt / K2 exist only for the FP32 path (null: not written).
-  pattern_ops_kernel<<<(unsigned)N * (unsigned)ceil_div(p->Kp, 256), 256, 0, ctx->stream>>>(
-      p->images, p->pix, p->cnorm, n2, N, p->Kp, p->Kraw, p->Kt, p->K2, p->flags, d_perm);
+  const int nqb = ceil_div(p->Kp, 256);
+  // once the tensor-core operands exist, their FP16 counts come from the same
+  // pass at the current K^2 scale (bind re-runs them if the new counts need
+  // another scale)
+  const bool fused = p->tc != nullptr && p->Kh != nullptr;
+  p->fused_k2_scale = fused ? p->k2_scale : 0.0f;
+  pattern_ops_kernel<<<(unsigned)N * (unsigned)nqb, 256, 0, ctx->stream>>>(
+      p->images, p->pix, p->cnorm, n2, N, p->Kp, p->Kraw, p->Kt, p->K2, p->flags, d_perm,
+      p->ksum_part, fused ? p->Kh : nullptr, fused ? p->K2hi : nullptr, fused ? p->K2lo : nullptr,
+      p->k2_scale);
   if ((rc = after_launch(ctx, "pattern_ops_kernel"))) return rc;
-  row_sum_kernel<<<N, 256, 0, ctx->stream>>>(p->Kraw, p->Kp, p->Kp, p->Ksum);
-  if ((rc = after_launch(ctx, "row_sum_kernel"))) return rc;
-  if (with_tc && p->tc) return tc_pattern_side(p, d_perm);
+  pattern_sums_kernel<<<ceil_div(N, 256), 256, 0, ctx->stream>>>(p->ksum_part, N, nqb, p->Ksum);
+  if ((rc = after_launch(ctx, "pattern_sums_kernel"))) return rc;
+  if (with_tc && p->tc) return tc_pattern_side(p, d_perm, fused);
   return EMC_OK;
 }
 
@@ -1053,18 +1095,24 @@ extern "C" int emc_plan_bind(emc_plan* p, const float* d_images, const int* d_ma
   if (!rc) rc = alloc_n(p, &p->cx, p->Kp);
   if (!rc) rc = alloc_n(p, &p->cy, p->Kp);
   if (!rc) rc = alloc_n(p, &p->cz, p->Kp);
-  if (!rc) rc = alloc_n(p, &p->Kraw, (size_t)N * p->Kp);
+  if (!rc) rc = alloc_n(p, &p->ksum_part, (size_t)N * ceil_div(p->Kp, 256));
+  if (!rc && p->d.precision == EMC_PREC_FP32) rc = alloc_n(p, &p->Kraw, (size_t)N * p->Kp);
   if (!rc) rc = alloc_n(p, &p->S, (size_t)p->Rp * p->Kp);
   if (!rc && p->d.precision == EMC_PREC_FP32) {
     rc = alloc_n(p, &p->Kt, (size_t)N * p->Kp);
     if (!rc) rc = alloc_n(p, &p->K2, (size_t)N * p->Kp);
+  }
+  // rows R..Rp of the slices stay zero: the expand writes rows < R only
+  if (!rc) {
+    const cudaError_t e =
+        cudaMemsetAsync(p->S, 0, sizeof(float) * (size_t)p->Rp * p->Kp, ctx->stream);
+    if (e != cudaSuccess) rc = cuda_fail(ctx, e, "plan_bind");
   }
   }
   if (rc) return rc;
   EMC_CUDA(ctx, cudaMemcpyAsync(p->pix, pix.data(), sizeof(int) * p->Kp, cudaMemcpyHostToDevice,
                                 ctx->stream));
   EMC_CUDA(ctx, cudaMemsetAsync(p->flags, 0, 16 * sizeof(int), ctx->stream));
-  EMC_CUDA(ctx, cudaMemsetAsync(p->S, 0, sizeof(float) * (size_t)p->Rp * p->Kp, ctx->stream));
   gather_coords_kernel<<<ceil_div(p->Kp, 256), 256, 0, ctx->stream>>>(p->pix, d_x, d_y, d_z, p->cx,
                                                                       p->cy, p->cz, p->Kp);
   if ((rc = after_launch(ctx, "gather_coords_kernel"))) return rc;

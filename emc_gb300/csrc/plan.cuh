@@ -39,7 +39,9 @@ struct emc_plan {
   float *cx = nullptr, *cy = nullptr, *cz = nullptr;  // [Kp]
 
   // pattern operands, rows of Kp (FP32 path)
-  float* Kraw = nullptr;  // k (x c_i when normalising)
+  float* Kraw = nullptr;  // k (x c_i when normalising); FP32 plans only
+  double* ksum_part = nullptr;  // [N][Kp / 256] block sums of k
+  float fused_k2_scale = 0.0f;  // K^2 scale of FP16 operands written by pattern_ops (0: none)
   float* Kt = nullptr;    // k if k > 1e-10 else 0
   float* K2 = nullptr;    // Kt^2
   float* Ksum = nullptr;  // [N] sum_p k
@@ -127,7 +129,7 @@ int prune_iterate(emc_plan* p, float* model, float* weight, float sigma, emc_ite
                   bool* handled);
 void prune_free(emc_plan* p);
 int prune_reset(emc_plan* p);
-int tc_pattern_side(emc_plan* p, const int* d_perm);
+int tc_pattern_side(emc_plan* p, const int* d_perm, bool counts_done = false);
 int tc_ensure_qlo(emc_plan* p);
 int pattern_side(emc_plan* p, const int* d_perm, bool with_tc);
 int tc_estep(emc_plan* p);

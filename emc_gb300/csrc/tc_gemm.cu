@@ -1142,20 +1142,25 @@ int tc_bind(emc_plan* p) {
                                        ms::SMEM_BYTES));
   }
   if (p->mstep_q_lo && (rc = tc_ensure_qlo(p))) return rc;
-  return tc_pattern_side(p, nullptr);
+  // counts already in FP16 from the bind's pattern pass when its scale holds
+  return tc_pattern_side(p, nullptr, p->fused_k2_scale == p->k2_scale);
 }
 
 // FP16 pattern operands for the pattern order perm (position -> input
 // pattern; nullptr: input order).
-int tc_pattern_side(emc_plan* p, const int* d_perm) {
+// counts_done: pattern_ops_kernel already wrote Kh / K2h / K2l at the
+// current scale (rows < N; the padding rows stay zero from the first bind).
+int tc_pattern_side(emc_plan* p, const int* d_perm, bool counts_done) {
   emc_ctx* ctx = p->ctx;
   const int N = p->d.n_images, Np = p->Np, Kp = p->Kp;
   const bool pois = p->d.diff == EMC_DIFF_TRUE_POISSON;
   int rc;
-  tc_pattern_ops_kernel<<<(unsigned)Np * (unsigned)ceil_div(Kp, 256), 256, 0, ctx->stream>>>(
-      p->images, p->pix, p->n2, N, Kp, p->Kh, pois ? nullptr : p->K2hi, p->K2lo, d_perm,
-      p->k2_scale);
-  if ((rc = after_launch(ctx, "tc_pattern_ops_kernel"))) return rc;
+  if (!counts_done) {
+    tc_pattern_ops_kernel<<<(unsigned)Np * (unsigned)ceil_div(Kp, 256), 256, 0, ctx->stream>>>(
+        p->images, p->pix, p->n2, N, Kp, p->Kh, pois ? nullptr : p->K2hi, p->K2lo, d_perm,
+        p->k2_scale);
+    if ((rc = after_launch(ctx, "tc_pattern_ops_kernel"))) return rc;
+  }
   if (!pois) tc_k2lo_flags_kernel<<<dim3(Kp / 32, Np / 128), 256, 0, ctx->stream>>>(p->K2lo, Kp, p->k2lo_any,
                                                                          Kp / 32);
   if ((rc = after_launch(ctx, "tc_k2lo_flags_kernel"))) return rc;

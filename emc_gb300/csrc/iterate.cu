@@ -226,7 +226,8 @@ __global__ void __launch_bounds__(256) slice_rows_kernel(
     const float* __restrict__ model, int side, const float* __restrict__ rot,
     const int* __restrict__ pix, const float* __restrict__ cx, const float* __restrict__ cy,
     const float* __restrict__ cz, int R, int Kp, float* __restrict__ S,
-    float* __restrict__ rot_cnt, float* __restrict__ rot_A, float* __restrict__ rot_ssum) {
+    float* __restrict__ rot_cnt, float* __restrict__ rot_A, float* __restrict__ rot_ssum,
+    RotOps ops) {
   const int r = blockIdx.x;
   __shared__ RotMat sR;
   if (threadIdx.x == 0) sR = quat_to_matrix(rot + 4 * (size_t)r);
@@ -244,7 +245,12 @@ __global__ void __launch_bounds__(256) slice_rows_kernel(
       }
       ss += fmaxf(s, kSliceFloor);
     }
-    S[(size_t)r * Kp + q] = s;
+    // the tensor path takes its FP16 operands straight from s; the FP32 path
+    // keeps the slices
+    if (ops.Gh)
+      rot_ops_store(ops, (size_t)r * Kp + q, s);
+    else
+      S[(size_t)r * Kp + q] = s;
   }
   __shared__ double sh[3][256];
   sh[0][threadIdx.x] = (double)cnt;
@@ -1097,13 +1103,13 @@ extern "C" int emc_plan_bind(emc_plan* p, const float* d_images, const int* d_ma
   if (!rc) rc = alloc_n(p, &p->cz, p->Kp);
   if (!rc) rc = alloc_n(p, &p->ksum_part, (size_t)N * ceil_div(p->Kp, 256));
   if (!rc && p->d.precision == EMC_PREC_FP32) rc = alloc_n(p, &p->Kraw, (size_t)N * p->Kp);
-  if (!rc) rc = alloc_n(p, &p->S, (size_t)p->Rp * p->Kp);
+  if (!rc && p->d.precision == EMC_PREC_FP32) rc = alloc_n(p, &p->S, (size_t)p->Rp * p->Kp);
   if (!rc && p->d.precision == EMC_PREC_FP32) {
     rc = alloc_n(p, &p->Kt, (size_t)N * p->Kp);
     if (!rc) rc = alloc_n(p, &p->K2, (size_t)N * p->Kp);
   }
   // rows R..Rp of the slices stay zero: the expand writes rows < R only
-  if (!rc) {
+  if (!rc && p->S) {
     const cudaError_t e =
         cudaMemsetAsync(p->S, 0, sizeof(float) * (size_t)p->Rp * p->Kp, ctx->stream);
     if (e != cudaSuccess) rc = cuda_fail(ctx, e, "plan_bind");
@@ -1145,14 +1151,15 @@ extern "C" int emc_plan_bind(emc_plan* p, const float* d_images, const int* d_ma
 
 static int plan_expand(emc_plan* p, const float* model) {
   emc_ctx* ctx = p->ctx;
+  const RotOps ops = tc_rot_ops(p);
   if (p->d.interp == EMC_INTERP_NEAREST)
     slice_rows_kernel<EMC_INTERP_NEAREST><<<p->d.n_rot, 256, 0, ctx->stream>>>(
         model, p->d.side, p->rot, p->pix, p->cx, p->cy, p->cz, p->d.n_rot, p->Kp, p->S,
-        p->rot_cnt, p->rot_A, p->rot_ssum);
+        p->rot_cnt, p->rot_A, p->rot_ssum, ops);
   else
     slice_rows_kernel<EMC_INTERP_TRILINEAR><<<p->d.n_rot, 256, 0, ctx->stream>>>(
         model, p->d.side, p->rot, p->pix, p->cx, p->cy, p->cz, p->d.n_rot, p->Kp, p->S,
-        p->rot_cnt, p->rot_A, p->rot_ssum);
+        p->rot_cnt, p->rot_A, p->rot_ssum, ops);
   return after_launch(ctx, "slice_rows_kernel");
 }
 
@@ -1575,7 +1582,6 @@ extern "C" int emc_plan_time_likelihood(emc_plan* p, const float* d_model, float
   if (d_model) {
     rc = set_sigma(p, sigma);
     if (!rc) rc = plan_expand(p, d_model);
-    if (!rc) rc = tc_estep_prepare(p);
   }
   if (!rc) rc = tc_time_estep(p, raster, first_tile, n_tiles, h_ms);
   if (!rc && h_total_tiles) *h_total_tiles = tc_estep_tiles(p);

@@ -132,9 +132,46 @@ int prune_reset(emc_plan* p);
 int tc_pattern_side(emc_plan* p, const int* d_perm, bool counts_done = false);
 int tc_ensure_qlo(emc_plan* p);
 int pattern_side(emc_plan* p, const int* d_perm, bool with_tc);
+// Rotation-side FP16 operands of the tensor-core likelihood, written by the
+// expand kernel straight from each slice value s (no FP32 slice buffer):
+// reference likelihood: M' = [s >= 1e-10], M'S * 2^-8, G = s / (s + c) and
+// H = 1 / (s + c) (c = 0.02; zero where s <= 0) as FP16 hi + lo; true Poisson:
+// log max(s, 1e-6) as FP16 hi + lo in Gh / Gl.  flags[0] |= 4 when M'S * 2^-8
+// leaves the FP16 range.
+struct RotOps {
+  __half *Mp = nullptr, *MSh = nullptr, *Gh = nullptr, *Gl = nullptr, *Hh = nullptr, *Hl = nullptr;
+  int* flags = nullptr;
+  int logs = 0;
+};
+
+__device__ __forceinline__ void rot_ops_store(const RotOps& o, size_t e, float s) {
+  if (o.logs) {
+    const float l = logf(fmaxf(s, 1e-6f));
+    const __half hi = __float2half_rn(l);
+    o.Gh[e] = hi;
+    o.Gl[e] = __float2half_rn(l - __half2float(hi));
+    return;
+  }
+  // (double)s > 1e-10 of the reference, as a float test: 1e-10f is the first
+  // float above 1e-10, so both agree for every float s
+  const bool mp = s >= 1e-10f;
+  const bool m = s > 0.0f;
+  const float ms = mp ? s * (1.0f / 256.0f) : 0.0f;
+  if (ms > 60000.0f) atomicOr(o.flags, 4);
+  const float h = m ? 1.0f / (s + 0.02f) : 0.0f;
+  const float g = m ? s * h : 0.0f;
+  const __half gh = __float2half_rn(g), hh = __float2half_rn(h);
+  o.Mp[e] = __float2half_rn(mp ? 1.0f : 0.0f);
+  o.MSh[e] = __float2half_rn(ms);
+  o.Gh[e] = gh;
+  o.Gl[e] = __float2half_rn(g - __half2float(gh));
+  o.Hh[e] = hh;
+  o.Hl[e] = __float2half_rn(h - __half2float(hh));
+}
+
+RotOps tc_rot_ops(emc_plan* p);  // the plan's operand buffers (all null for FP32 plans)
 int tc_estep(emc_plan* p);
 int tc_autotune(emc_plan* p, int waves, int* best, float* best_ms);
-int tc_estep_prepare(emc_plan* p);  // rotation operands of the likelihood from the slices
 int tc_estep_tiles(emc_plan* p);    // tiles of the full likelihood grid
 int tc_time_estep(emc_plan* p, int raster, int first, int count, float* ms);
 int tc_mstep(emc_plan* p, float* model, float* weight);

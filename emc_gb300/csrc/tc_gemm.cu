@@ -84,8 +84,6 @@ static int make_map(emc_ctx* ctx, CUtensorMap* map, const void* base, uint64_t r
 
 // ---------------------------------------------------- pattern operands ---
 
-constexpr float kMSScale = 1.0f / 256.0f;  // (M' S) * 2^-8 keeps slices below 2^24 in range
-
 // Counts -> FP16 operands, rows of Kp (patterns padded to Np with zeros):
 // Kh = fp16(k) (k itself up to 2048; larger counts rounded to 11 significant
 // bits), K2h + K2l = Kh^2 * k2_scale exactly (Kh^2 has at most 22 significant
@@ -144,53 +142,6 @@ __global__ void transpose_h_kernel(const __half* __restrict__ in, int rows, int 
   for (int y = threadIdx.y; y < 32; y += blockDim.y) {
     const int c = c0 + y, r = r0 + threadIdx.x;
     if (c < cols && r < rows) out[(size_t)c * rows + r] = t[threadIdx.x][y];
-  }
-}
-
-// ---------------------------------------------------- rotation operands --
-constexpr float kPoisCf = 0.02f;
-
-// From the compacted slices S [Rp][Kp] (FP32): the six FP16 rotation-side
-// operands, each [Rp][Kp]: M' = [s > 1e-10], (M' s) 2^-8 hi, G = [s > 0]
-// s/(s+c) hi/lo, H = [s > 0] /(s+c) hi/lo.  flags[0] |= 4 when a slice value
-// does not fit the scaled FP16 range.
-__global__ void tc_rot_ops_kernel(const float* __restrict__ S, size_t n, __half* __restrict__ Mp,
-                                  __half* __restrict__ MSh, __half* __restrict__ Gh,
-                                  __half* __restrict__ Gl, __half* __restrict__ Hh,
-                                  __half* __restrict__ Hl, int* __restrict__ flags) {
-  const size_t stride = (size_t)gridDim.x * blockDim.x;
-  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += stride) {
-    const float s = S[e];
-    // (double)s > 1e-10 of the reference, as a float test: 1e-10f is the
-    // first float above 1e-10, so both agree for every float s
-    const bool mp = s >= 1e-10f;
-    const bool m = s > 0.0f;
-    const float ms = mp ? s * kMSScale : 0.0f;
-    if (ms > 60000.0f) atomicOr(flags, 4);
-    const float h = m ? 1.0f / (s + kPoisCf) : 0.0f;
-    const float g = m ? s * h : 0.0f;
-    const __half gh = __float2half_rn(g), hh = __float2half_rn(h);
-    Mp[e] = __float2half_rn(mp ? 1.0f : 0.0f);
-    MSh[e] = __float2half_rn(ms);
-    Gh[e] = gh;
-    Gl[e] = __float2half_rn(g - __half2float(gh));
-    Hh[e] = hh;
-    Hl[e] = __float2half_rn(h - __half2float(hh));
-  }
-}
-
-// True-Poisson rotation operand: log max(s, floor) as FP16 hi + lo [Rp][Kp]
-// (|log| <= 14 for slices below 2^20; hi + lo carries ~22 bits).
-constexpr float kSliceFloorT = 1e-6f;  // the FP32 path's floor for unknown voxels
-
-__global__ void tc_rot_logs_kernel(const float* __restrict__ S, size_t n, __half* __restrict__ Lh,
-                                   __half* __restrict__ Ll) {
-  const size_t stride = (size_t)gridDim.x * blockDim.x;
-  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += stride) {
-    const float l = logf(fmaxf(S[e], kSliceFloorT));
-    const __half hi = __float2half_rn(l);
-    Lh[e] = hi;
-    Ll[e] = __float2half_rn(l - __half2float(hi));
   }
 }
 
@@ -1108,8 +1059,11 @@ int tc_bind(emc_plan* p) {
       if (!rc) rc = plan_alloc(p, (void**)&p->k2lo_any, (size_t)(Np / 128) * (Kp / 32));
     }
     __half** rot_ops[6] = {&st->Gh, &st->Gl, &st->Mp, &st->MSh, &st->Hh, &st->Hl};
-    for (int j = 0; j < (pois ? 2 : 6); ++j)
+    for (int j = 0; j < (pois ? 2 : 6); ++j) {
       if (!rc) rc = plan_alloc(p, (void**)rot_ops[j], rk * 2);
+      // rows R..Rp stay zero: the expand writes the operands of rows < R
+      if (!rc) EMC_CUDA(ctx, cudaMemsetAsync(*rot_ops[j], 0, rk * 2, ctx->stream));
+    }
     if (!rc) rc = plan_alloc(p, (void**)&p->Qh, (size_t)Rp * Np * 2);
     if (!rc) rc = plan_alloc(p, (void**)&p->qscale, (size_t)Rp * 4);
     if (!rc) rc = plan_alloc(p, (void**)&st->status, 64);
@@ -1217,20 +1171,6 @@ static int estep_pois_launch(emc_plan* p, int raster, int first, int count, bool
   return after_launch(ctx, "tc_estep_pois_kernel");
 }
 
-// The rotation-side FP16 operands of the likelihood from the slices S.
-static int estep_operands(emc_plan* p) {
-  emc_ctx* ctx = p->ctx;
-  TcState* st = state(p);
-  const size_t rk = (size_t)p->Rp * p->Kp;
-  if (p->d.diff == EMC_DIFF_TRUE_POISSON) {
-    tc_rot_logs_kernel<<<ctx->sm_count * 8, 256, 0, ctx->stream>>>(p->S, rk, st->Gh, st->Gl);
-    return after_launch(ctx, "tc_rot_logs_kernel");
-  }
-  tc_rot_ops_kernel<<<ctx->sm_count * 8, 256, 0, ctx->stream>>>(p->S, rk, st->Mp, st->MSh, st->Gh,
-                                                                st->Gl, st->Hh, st->Hl, p->flags);
-  return after_launch(ctx, "tc_rot_ops_kernel");
-}
-
 static int estep_launch(emc_plan* p, int raster, int first, int count, bool full) {
   if (p->d.diff == EMC_DIFF_TRUE_POISSON) return estep_pois_launch(p, raster, first, count, full);
   emc_ctx* ctx = p->ctx;
@@ -1297,10 +1237,25 @@ static int estep_launch(emc_plan* p, int raster, int first, int count, bool full
   return after_launch(ctx, "tc_estep_kernel");
 }
 
-int tc_estep(emc_plan* p) {
-  int rc = estep_operands(p);
-  if (rc) return rc;
-  return estep_launch(p, p->estep_raster, 0, INT_MAX, false);
+// The rotation operands were written by the expand (rot_ops_store).
+int tc_estep(emc_plan* p) { return estep_launch(p, p->estep_raster, 0, INT_MAX, false); }
+
+RotOps tc_rot_ops(emc_plan* p) {
+  RotOps o;
+  if (!p->tc) return o;
+  TcState* st = state(p);
+  o.flags = p->flags;
+  o.Gh = st->Gh;
+  o.Gl = st->Gl;
+  if (p->d.diff == EMC_DIFF_TRUE_POISSON) {
+    o.logs = 1;
+  } else {
+    o.Mp = st->Mp;
+    o.MSh = st->MSh;
+    o.Hh = st->Hh;
+    o.Hl = st->Hl;
+  }
+  return o;
 }
 
 // The likelihood lo terms in force: bit 0 G lo, bit 1 H lo (auto: H lo when
@@ -1355,12 +1310,11 @@ int tc_estep_tiles(emc_plan* p) {
 // x SM-count tiles inside the grid (at 30 % and 65 % of its order; the whole
 // grid when it is smaller) and scored by the slower window, so an order that
 // is fast only at times loses to a steady one.  The rotation operands are
-// rebuilt from the slices of the last expansion; the timed launches
-// overwrite responsibilities and scaling of the tiles they cover.
+// those of the last expansion; the timed launches overwrite
+// responsibilities and scaling of the tiles they cover.
 int tc_autotune(emc_plan* p, int waves, int* best, float* best_ms) {
   emc_ctx* ctx = p->ctx;
-  int rc = estep_operands(p);
-  if (rc) return rc;
+  int rc = EMC_OK;
   const bool pois = p->d.diff == EMC_DIFF_TRUE_POISSON;
   const bool pair = !pois && estep_uses_pair(p);
   const int n_pt = pair ? (p->Np / 128 + 1) / 2 : p->Np / 128;
@@ -1401,7 +1355,6 @@ int tc_autotune(emc_plan* p, int waves, int* best, float* best_ms) {
   return EMC_OK;
 }
 
-int tc_estep_prepare(emc_plan* p) { return estep_operands(p); }
 
 int tc_mstep(emc_plan* p, float* model, float* weight) {
   emc_ctx* ctx = p->ctx;

@@ -661,25 +661,55 @@ __global__ void __launch_bounds__(kMprepThreads) mprep_kernel(
   // (P = 0), 1 evaluated, 2 evaluated margin tile (its mass is summed)
   const unsigned char* ts = tstate ? tstate + (r >> 7) : nullptr;
   float t = 0.0f, b = 0.0f, qmax = 0.0f, mg = 0.0f;
-  for (int i = threadIdx.x; i < N; i += blockDim.x) {
-    const size_t e = (size_t)r * N + i;
-    const int st = ts ? ts[(size_t)(i >> 7) * n_rt] : 1;
-    float P = 0.0f, f = 0.0f;
+  // one element: P = exp(L - lse) (0 outside the evaluated tiles), q = P / phi
+  // (x c_i for the FP16 operand); returns q and stores P
+  auto elem = [&](int i, int st, float l, float f, float2 li, float ks, float cn) -> float {
+    float P = 0.0f;
     if (st) {
-      const float2 li = lse2[i];
-      const float l = L[e];
       if (isfinite(li.x) && l > -INFINITY) P = expf((l - li.x) - li.y);
-      f = PHI[e];
       if (st == 2) mg += P;
+    } else {
+      f = 0.0f;
     }
-    L[e] = P;
     float q = f > 0.0f ? __fdiv_rn(P, f) : 0.0f;
     t += P;
-    b = __fmaf_rn(q, __ldg(Ksum + i), b);
-    if (Qh) q = __fmul_rn(q, __ldg(cnorm + i));
+    b = __fmaf_rn(q, ks, b);
+    if (Qh) q = __fmul_rn(q, cn);
     qmax = fmaxf(qmax, q);
     if (Q) Q[(size_t)r * ldq + i] = q;
     if (stage) qrow[i] = q;
+    return P;
+  };
+  if ((N & 3) == 0) {
+    // 16-byte rows: four elements per load keep enough bytes in flight to
+    // approach HBM bandwidth (4-tuples never straddle a 128-pattern tile)
+    float4* L4 = reinterpret_cast<float4*>(L + (size_t)r * N);
+    const float4* F4 = reinterpret_cast<const float4*>(PHI + (size_t)r * N);
+    const float4* S4 = reinterpret_cast<const float4*>(lse2);
+    const float4* K4 = reinterpret_cast<const float4*>(Ksum);
+    const float4* C4 = reinterpret_cast<const float4*>(cnorm);
+    for (int j = threadIdx.x; j < N / 4; j += blockDim.x) {
+      const int i = 4 * j;
+      const int st = ts ? ts[(size_t)(i >> 7) * n_rt] : 1;
+      const float4 l = L4[j];
+      const float4 f = st ? F4[j] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      const float4 s01 = S4[2 * j], s23 = S4[2 * j + 1];
+      const float4 ks = __ldg(K4 + j), cn = __ldg(C4 + j);
+      float4 P;
+      P.x = elem(i, st, l.x, f.x, make_float2(s01.x, s01.y), ks.x, cn.x);
+      P.y = elem(i + 1, st, l.y, f.y, make_float2(s01.z, s01.w), ks.y, cn.y);
+      P.z = elem(i + 2, st, l.z, f.z, make_float2(s23.x, s23.y), ks.z, cn.z);
+      P.w = elem(i + 3, st, l.w, f.w, make_float2(s23.z, s23.w), ks.w, cn.w);
+      L4[j] = P;
+    }
+  } else {
+    for (int i = threadIdx.x; i < N; i += blockDim.x) {
+      const size_t e = (size_t)r * N + i;
+      const int st = ts ? ts[(size_t)(i >> 7) * n_rt] : 1;
+      const float l = L[e];
+      const float f = st ? PHI[e] : 0.0f;
+      L[e] = elem(i, st, l, f, lse2[i], __ldg(Ksum + i), __ldg(cnorm + i));
+    }
   }
   if (Q)
     for (int i = N + threadIdx.x; i < ldq; i += blockDim.x) Q[(size_t)r * ldq + i] = 0.0f;
@@ -710,20 +740,28 @@ __global__ void __launch_bounds__(kMprepThreads) mprep_kernel(
   int ex = mx > 0.0f ? 14 - ilogbf(mx) - 1 : 0;
   ex = max(-100, min(100, ex));
   const float up = ldexpf(1.0f, ex);
-  for (int i = threadIdx.x; i < ldq; i += blockDim.x) {
-    float q = 0.0f;
-    if (i < N) {
-      if (stage) {
-        q = __fmul_rn(qrow[i], up);
-      } else {  // re-read the row (L now holds P)
-        const size_t e = (size_t)r * N + i;
-        const float f = PHI[e];
-        q = f > 0.0f ? __fmul_rn(__fmul_rn(__fdiv_rn(L[e], f), __ldg(cnorm + i)), up) : 0.0f;
-      }
+  auto qval = [&](int i) -> float {
+    if (i >= N) return 0.0f;
+    if (stage) return __fmul_rn(qrow[i], up);
+    // re-read the row (L now holds P)
+    const size_t e = (size_t)r * N + i;
+    const float f = PHI[e];
+    return f > 0.0f ? __fmul_rn(__fmul_rn(__fdiv_rn(L[e], f), __ldg(cnorm + i)), up) : 0.0f;
+  };
+  // ldq is a multiple of 128: four FP16 values (8 bytes) per store
+  for (int j = threadIdx.x; j < ldq / 4; j += blockDim.x) {
+    const int i = 4 * j;
+    union Pack4 {
+      __half h[4];
+      uint2 u;
+    } hi, lo;
+    for (int c = 0; c < 4; ++c) {
+      const float q = qval(i + c);
+      hi.h[c] = __float2half_rn(q);
+      lo.h[c] = __float2half_rn(q - __half2float(hi.h[c]));
     }
-    const __half hi = __float2half_rn(q);
-    Qh[(size_t)r * ldq + i] = hi;
-    if (Ql) Ql[(size_t)r * ldq + i] = __float2half_rn(q - __half2float(hi));
+    *reinterpret_cast<uint2*>(Qh + (size_t)r * ldq + i) = hi.u;
+    if (Ql) *reinterpret_cast<uint2*>(Ql + (size_t)r * ldq + i) = lo.u;
   }
   if (threadIdx.x == 0) qscale[r] = ldexpf(1.0f, -ex);
 }
@@ -1070,17 +1108,21 @@ extern "C" int emc_plan_bind(emc_plan* p, const float* d_images, const int* d_ma
   EMC_CUDA(ctx, cudaMemcpyAsync(hmask.data(), d_mask, sizeof(int) * n2, cudaMemcpyDeviceToHost,
                                 ctx->stream));
   EMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  // a re-bind with the same mask keeps the compacted pixel list
+  const bool same_mask = prev_P != 0 && hmask == p->h_mask;
   std::vector<int> pix;
-  for (int q = 0; q < n2; ++q) {
-    EMC_REQUIRE(ctx, hmask[q] == 0 || hmask[q] == 1, "plan_bind: mask values must be 0 or 1");
-    if (hmask[q]) pix.push_back(q);
-  }
-  EMC_REQUIRE(ctx, !pix.empty(), "plan_bind: mask is empty");
-  // Compacted pixels in order of detector radius: the bright low-q pixels,
-  // the only ones whose k^2 needs a second FP16 term, then share a few
-  // k-blocks of the tensor-core E-step (the order is otherwise free: every
-  // compacted array uses it consistently).
-  {
+  if (same_mask) {
+    pix = p->h_pix;
+  } else {
+    for (int q = 0; q < n2; ++q) {
+      EMC_REQUIRE(ctx, hmask[q] == 0 || hmask[q] == 1, "plan_bind: mask values must be 0 or 1");
+      if (hmask[q]) pix.push_back(q);
+    }
+    EMC_REQUIRE(ctx, !pix.empty(), "plan_bind: mask is empty");
+    // Compacted pixels in order of detector radius: the bright low-q pixels,
+    // the only ones whose k^2 needs a second FP16 term, then share a few
+    // k-blocks of the tensor-core E-step (the order is otherwise free: every
+    // compacted array uses it consistently).
     const int side = p->d.side;
     auto r2 = [side](int q) {
       const double dx = (double)(q % side) - side / 2 + 0.5, dy = (double)(q / side) - side / 2 + 0.5;
@@ -1116,8 +1158,13 @@ extern "C" int emc_plan_bind(emc_plan* p, const float* d_images, const int* d_ma
   }
   }
   if (rc) return rc;
-  EMC_CUDA(ctx, cudaMemcpyAsync(p->pix, pix.data(), sizeof(int) * p->Kp, cudaMemcpyHostToDevice,
-                                ctx->stream));
+  if (!same_mask) {
+    p->h_mask = hmask;
+    p->h_pix.assign(pix.begin(), pix.begin() + p->P_eff);
+    // pageable source: staged before the call returns
+    EMC_CUDA(ctx, cudaMemcpyAsync(p->pix, pix.data(), sizeof(int) * p->Kp,
+                                  cudaMemcpyHostToDevice, ctx->stream));
+  }
   EMC_CUDA(ctx, cudaMemsetAsync(p->flags, 0, 16 * sizeof(int), ctx->stream));
   gather_coords_kernel<<<ceil_div(p->Kp, 256), 256, 0, ctx->stream>>>(p->pix, d_x, d_y, d_z, p->cx,
                                                                       p->cy, p->cz, p->Kp);

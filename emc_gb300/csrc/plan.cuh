@@ -41,6 +41,7 @@ struct emc_plan {
   // pattern operands, rows of Kp (FP32 path)
   float* Kraw = nullptr;  // k (x c_i when normalising); FP32 plans only
   double* ksum_part = nullptr;  // [N][Kp / 256] block sums of k
+  std::vector<int> h_mask, h_pix;  // the bound mask and its compacted pixels (re-binds)
   float fused_k2_scale = 0.0f;  // K^2 scale of FP16 operands written by pattern_ops (0: none)
   float* Kt = nullptr;    // k if k > 1e-10 else 0
   float* K2 = nullptr;    // Kt^2

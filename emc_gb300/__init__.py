@@ -413,6 +413,7 @@ class Plan:
     OPT_COUNTS_ROUND = 5
     OPT_ESTEP_RASTER = 6
     OPT_ESTEP_PAIR = 7
+    OPT_MSTEP_RASTER = 8
 
     def set_option(self, option: int, value: int):
         self.ctx._check(self._lib.emc_plan_set_option(self._h, option, value), "plan_set_option")

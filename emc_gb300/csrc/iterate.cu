@@ -1572,6 +1572,12 @@ extern "C" int emc_plan_set_option(emc_plan* p, int option, int value) {
     p->estep_raster = value;
     return EMC_OK;
   }
+  if (option == EMC_OPT_MSTEP_RASTER) {
+    EMC_REQUIRE(ctx, value != 0 && value >= -4096 && value <= 4096,
+                "plan_set_option: M-step raster %d", value);
+    p->mstep_raster = value;
+    return EMC_OK;
+  }
   if (option == EMC_OPT_ESTEP_PAIR) {
     EMC_REQUIRE(ctx, value == 0 || value == 1, "plan_set_option: pair %d", value);
     p->estep_pair = value;

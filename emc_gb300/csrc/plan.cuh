@@ -103,6 +103,7 @@ struct emc_plan {
   int mstep_q_lo = 0;     // tensor M-step: Q as FP16 hi + lo (1) or hi only (0)
   int estep_raster = 8;     // tensor E-step tile order (EMC_OPT_ESTEP_RASTER)
   int estep_pair = 1;       // full scans on CTA pairs (EMC_OPT_ESTEP_PAIR)
+  int mstep_raster = -16;   // tensor M-step tile order (EMC_OPT_MSTEP_RASTER)
   int mstep_aggregate = 0;  // tensor M-step: warp-aggregated float atomics (nearest)
 
   std::vector<void*> allocs;

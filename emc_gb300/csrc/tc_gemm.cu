@@ -751,11 +751,11 @@ constexpr int STAGE_BYTES = 2 * A_BYTES + B_BYTES;
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 256 + 1024;
 constexpr int EPI_WARPS = 8;          // two per TMEM lane quarter, 128 columns each
 constexpr int THREADS = 64 + 32 * EPI_WARPS;
-constexpr int GROUP = 8;
 }  // namespace ms
 
 struct TcMstepArgs {
   int R, Kp, Np, P_eff, n_qt, n_rt, nkb, n_tiles;
+  int raster;  // tile order (raster_tile over pixel tiles x rotation tiles)
   const float* T;
   const float* qscale;  // [R] 2^-e_r
   const float* rot;
@@ -854,14 +854,14 @@ __device__ __forceinline__ void tc_insert(const TcMstepArgs& a, const RotMat& R,
   }
 }
 
-// Tile t of the grouped raster: GROUP rotation tiles share each pixel tile.
+// Tile t of the grouped raster (raster_tile over pixel tiles x rotation
+// tiles; the default -16: groups of 16 pixel tiles run through all rotation
+// tiles, 5-6 % faster than groups of 8 rotation tiles at 128^3 and 256^3).
 __device__ __forceinline__ void ms_tile(const TcMstepArgs& a, int t, int& r0, int& q0) {
-  const int per_group = ms::GROUP * a.n_qt;
-  const int g = t / per_group, within = t % per_group;
-  const int rt0 = g * ms::GROUP;
-  const int gsz = min(ms::GROUP, a.n_rt - rt0);
-  r0 = (rt0 + within % gsz) * ms::BM;
-  q0 = (within / gsz) * ms::BN;
+  int qt, rt;
+  raster_tile(t, a.raster, a.n_qt, a.n_rt, qt, rt);
+  r0 = rt * ms::BM;
+  q0 = qt * ms::BN;
 }
 
 // Persistent: CTA b takes tiles b, b + grid, ...  The k-block ring runs on
@@ -1367,6 +1367,7 @@ int tc_mstep(emc_plan* p, float* model, float* weight) {
   a.n_qt = p->Kp / ms::BN + (p->Kp % ms::BN ? 1 : 0);
   a.n_rt = p->Rp / ms::BM;
   a.nkb = p->Np / ms::BK;
+  a.raster = p->mstep_raster;
   a.T = p->T;
   a.qscale = p->qscale;
   a.rot = p->rot;

@@ -455,6 +455,13 @@ int emc_batch_destroy(emc_batch* batch);
  * bounds the single-CTA kernel); 0 runs every scan on single CTAs.  Pruned
  * iterations always use single CTAs.  Results are the same either way. */
 #define EMC_OPT_ESTEP_PAIR 7
+/* EMC_OPT_MSTEP_RASTER: order of the persistent tensor-core M-step's
+ * (rotation tile, pixel tile) work: g > 0 groups of g rotation tiles running
+ * through all pixel tiles, g < 0 (default -16) groups of -g pixel tiles
+ * running through all rotation tiles; |g| <= 4096.  Results do not depend
+ * on it (with deterministic insertion, bit for bit).  At 128^3 and 256^3 the
+ * default is 5-6 % faster than groups of 8 rotation tiles. */
+#define EMC_OPT_MSTEP_RASTER 8
 int emc_plan_set_option(emc_plan* plan, int option, int value);
 /* Tile-order autotuner of the tensor-core likelihood kernel: expands d_model
  * (sigma as in emc_iterate), times the kernel for each candidate

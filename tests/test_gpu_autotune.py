@@ -82,3 +82,21 @@ def test_autotune_fp32_plan_and_bad_orders(ctx, cuda, prob):
         with pytest.raises(E.EmcError):
             plan.set_option(E.Plan.OPT_ESTEP_RASTER, bad)
     plan.close()
+
+
+def test_mstep_orders_give_identical_iterations(ctx, cuda, prob):
+    """The M-step's tile order (EMC_OPT_MSTEP_RASTER) changes which CTA
+    inserts which tile when, never the deterministic sums."""
+    plan, m0 = bound(ctx, prob, cuda, precision=E.PREC_MIXED)
+    outs = []
+    for g in (8, 1, 3, -2, -64, 4096):
+        plan.set_option(E.Plan.OPT_MSTEP_RASTER, g)
+        m, w = m0.clone(), torch.empty_like(m0)
+        plan.iterate(m, w, 0.3)
+        outs.append((m.cpu().numpy(), w.cpu().numpy()))
+    for m, w in outs[1:]:
+        assert np.array_equal(m, outs[0][0]) and np.array_equal(w, outs[0][1])
+    for bad in (0, 4097):
+        with pytest.raises(E.EmcError):
+            plan.set_option(E.Plan.OPT_MSTEP_RASTER, bad)
+    plan.close()

@@ -1,7 +1,7 @@
 // C wrappers around the reference's own host functions (emc_cuda.cu,
 // emc_atomic.cu compiled unchanged from the reference tree for sm_103a by
 // oracle/build_ref.sh --kernels).  TEST INFRASTRUCTURE ONLY: used once, on a
-// GPU machine, by tests/golden/make_ref_kernel_golden.py to record the reference
+// machine with a GB300, by tests/golden/make_ref_kernel_golden.py to record the reference
 // kernels' outputs as golden fixtures that pin the oracle.  Each wrapper
 // fills the spimage structs the reference reads sizes from, calls the
 // reference function and synchronises.

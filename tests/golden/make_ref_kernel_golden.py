@@ -1,12 +1,13 @@
 """Records the reference's own CUDA kernels' outputs as golden fixtures.
 
-Runs on a GPU machine.  Builds oracle/_ref/libemc_ref_kernels.so from the
-reference sources (emc_cuda.cu, emc_atomic.cu compiled unchanged for sm_103a
-behind oracle/ref_harness.cu) -- from $EMC_REF_DIR, else the reference tree,
-else the staged copy in baseline/_ref/src -- feeds it a small seeded problem
-and writes inputs and outputs to gpurun_out/ref_kernels_golden.npz, which is
-committed as tests/golden/ref_kernels_golden.npz.
-    python tests/golden/make_ref_kernel_golden.py
+Runs on a machine with a GB300.  Builds oracle/_ref/libemc_ref_kernels.so
+from the reference sources (emc_cuda.cu, emc_atomic.cu compiled unchanged for
+sm_103a behind oracle/ref_harness.cu) -- from $EMC_REF_DIR, else the reference
+tree, else the staged copy in baseline/_ref/src -- feeds it a small seeded
+problem and writes inputs and outputs to the file given as the argument
+(default ref_kernels_golden.npz in the working directory), which is committed
+as tests/golden/ref_kernels_golden.npz.
+    python tests/golden/make_ref_kernel_golden.py [out.npz]
 """
 from __future__ import annotations
 
@@ -92,8 +93,8 @@ def main():
     out["avg_before"] = np.float32(lib.ref_model_average(ptr(new_m), s ** 3))
     assert lib.ref_normalize_model(s, ptr(new_m)) == 0
     out["normalized"] = new_m.cpu().numpy()
-    dst = ROOT / "gpurun_out" / "ref_kernels_golden.npz"
-    dst.parent.mkdir(exist_ok=True)
+    dst = Path(sys.argv[1] if len(sys.argv) > 1 else "ref_kernels_golden.npz").resolve()
+    dst.parent.mkdir(parents=True, exist_ok=True)
     np.savez_compressed(dst, **out)
     print(f"wrote {dst} ({dst.stat().st_size} bytes)")
 

@@ -20,7 +20,7 @@ cpu_baseline / --impl reference
           the oracle's C restatement of the reference kernels (OpenMP, all
           host threads) on a bounded sample of the same workload.
 Multi-GPU: replicas only (one independent iteration per rank; the reference's
-rotation split has no exchange to accelerate on single-GPU boxes).
+rotation split has no exchange to accelerate on single-GPU machines).
 """
 from __future__ import annotations
 
@@ -126,11 +126,12 @@ class ClockSampler:
     def __init__(self, index):
         self.index = index
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+        import tempfile
+        fd, self.path = tempfile.mkstemp(prefix="emc_clocks_", suffix=".csv")
+        os.close(fd)
 
     def start(self):
         try:
-            os.makedirs(os.path.dirname(self.path), exist_ok=True)
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index),

@@ -1222,8 +1222,13 @@ static int estep_launch(emc_plan* p, int raster, int first, int count, bool full
     cfg.numAttrs = 1;
     const cudaError_t e = cudaLaunchKernelEx(&cfg, tc_estep_pair_kernel, st->mK, st->mK2h, st->mK2l,
                                              rm[0], rm[1], rm[2], st->gl64, rm[4], a);
-    if (e != cudaSuccess) return cuda_fail(ctx, e, "tc_estep_pair_kernel launch");
-    return after_launch(ctx, "tc_estep_pair_kernel");
+    if (e == cudaSuccess) return after_launch(ctx, "tc_estep_pair_kernel");
+    // a refused launch configuration (a GPU or partition that cannot
+    // co-schedule the pairs) is not a sticky error: single CTAs from now on
+    (void)cudaGetLastError();
+    p->estep_pair = 0;
+    first *= 2;  // the same region of the grid in single-CTA tiles
+    count = count > INT_MAX / 2 ? INT_MAX : 2 * count;
   }
   const int total = a.n_pt * a.n_rt;
   first = a.tiles ? 0 : std::max(0, std::min(first, total));

@@ -60,3 +60,33 @@ def test_coordinates_geometry(built):
     # ~1e-3 voxels of cancellation noise on z (a tenth of a voxel at the rim)
     assert np.abs(z - want).max() < 1e-3
     assert (z >= 0).all()  # 1 - cos rounds to 0 in float near the beam
+
+
+def test_option_numbers_match_the_header(built):
+    """Plan.OPT_* carries the header's EMC_OPT_* numbers."""
+    import re
+    from pathlib import Path
+
+    import emc_gb300 as E
+    hdr = (Path(__file__).resolve().parents[1] / "include" / "emc_gb300.h").read_text()
+    opts = {m.group(1): int(m.group(2))
+            for m in re.finditer(r"#define EMC_OPT_([A-Z0-9_]+) (-?\d+)", hdr)}
+    assert len(opts) >= 7
+    for name, value in opts.items():
+        assert getattr(E.Plan, "OPT_" + name) == value, name
+
+
+def test_heldout_patterns_share_the_particle():
+    """pattern_seed draws new orientations, scales and counts of the same
+    particle and detector."""
+    from emc_gb300 import synthetic as S
+    import dataclasses
+    cfg = dataclasses.replace(S.tiny(side=24, n_images=20, rot_n=1), photons=300)
+    rot = (np.zeros((1, 4), np.float32), np.ones(1, np.float32))
+    coords = tuple(np.zeros(24 * 24, np.float32) + v for v in (0.0, 0.0, 0.0))
+    a = S.make_problem(cfg, coords=coords, rotations=rot)
+    b = S.make_problem(cfg, coords=coords, rotations=rot, pattern_seed=1)
+    c = S.make_problem(cfg, coords=coords, rotations=rot, pattern_seed=1)
+    assert np.array_equal(a.true_model, b.true_model) and np.array_equal(a.mask, b.mask)
+    assert not np.allclose(a.true_quats, b.true_quats)
+    assert np.array_equal(b.true_quats, c.true_quats) and np.array_equal(b.images, c.images)

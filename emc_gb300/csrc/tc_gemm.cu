@@ -1227,7 +1227,7 @@ static int estep_launch(emc_plan* p, int raster, int first, int count, bool full
     // co-schedule the pairs) is not a sticky error: single CTAs from now on
     (void)cudaGetLastError();
     p->estep_pair = 0;
-    first *= 2;  // the same region of the grid in single-CTA tiles
+    first *= 2;  // about the same part of the grid, in single-CTA tiles
     count = count > INT_MAX / 2 ? INT_MAX : 2 * count;
   }
   const int total = a.n_pt * a.n_rt;

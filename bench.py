@@ -74,9 +74,12 @@ def parse():
                          "0 (default): chosen by emc_plan_autotune before the warm-up")
     ap.add_argument("--plain-steps", type=int, default=2)
     ap.add_argument("--e2e-steps", type=int, default=4)
-    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0,
+                    help="target duration of the FP64 host-oracle baseline (cpu_baseline)")
+    ap.add_argument("--ref-seconds", type=float, default=100.0,
+                    help="--impl reference: target duration of all warm-up + timed steps")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--ref-gpu-chunk", type=int, default=256,
+    ap.add_argument("--ref-gpu-chunk", type=int, default=128,
                     help="--impl reference: rotations per timed chunk of the reference's own "
                          "CUDA kernels (0: skip them)")
     ap.add_argument("--prune-steps", type=int, default=4,
@@ -224,33 +227,48 @@ def workload_desc(prob, precision, insert):
                   f"per step)"}
 
 
-# ---------------------------------------------------- CPU (oracle) leg ----
-def cpu_leg(prob, seconds):
-    """Times the oracle's restatement of the reference path (scaling,
-    likelihood, LSE, M-step, insertion, divide, normalise) on a sample of
-    rotations x patterns of the workload, full detector.  Returns pairs/s."""
-    import numpy as np
+# ---------------------------------------------------- CPU (oracle) legs ----
+def b1_leg(prob, seconds):
+    """The FP64 host oracle in GEMM form (oracle.fused_iteration_fp64: numpy /
+    OpenBLAS on all host threads) on a chunk of rotations x ALL patterns of the
+    workload, full detector: the fused iteration's semantics evaluated in
+    FP64.  The chunk is sized from a probe so the timed run takes about
+    `seconds`.  Returns the cpu_baseline object."""
     from oracle import oracle as O
-    s = prob.cfg.side
+    s, R, N = prob.cfg.side, prob.quats.shape[0], prob.images.shape[0]
     cores = os.cpu_count() or 1
-    os.environ.setdefault("OMP_NUM_THREADS", str(cores))
 
-    def run(nr, ni):
+    def run(nr):
         t0 = time.perf_counter()
-        O.ref_iteration(prob.init_model, prob.images[:ni], prob.mask, prob.x, prob.y, prob.z,
-                        prob.quats[:nr], prob.weights[:nr], O.sigma_at(0), s)
+        O.fused_iteration_fp64(prob.init_model, prob.images, prob.mask, prob.x, prob.y, prob.z,
+                               prob.quats[:nr], prob.weights[:nr], float(O.sigma_at(0)), s)
         return time.perf_counter() - t0
 
-    nr, ni = 8, 64
-    t = run(nr, ni)
-    scale = max(1.0, seconds / max(t, 1e-3))
-    ni2 = int(min(prob.images.shape[0], ni * max(1.0, scale ** 0.5)))
-    nr2 = int(min(prob.quats.shape[0], nr * max(1.0, scale / (ni2 / ni))))
-    t2 = run(nr2, ni2)
-    return dict(value=nr2 * ni2 / t2, unit=UNIT, cores=cores, kind="port",
-                sample=f"{nr2} rotations x {ni2} patterns of the {prob.cfg.name} workload, "
-                       f"full {s}x{s} detector, one reference-semantics iteration "
-                       f"(oracle/emc_oracle.c, OpenMP), {t2:.1f} s"), t2
+    nr0 = min(R, 64)
+    t0 = run(nr0)
+    nr = int(min(R, max(nr0, nr0 * seconds / max(t0, 1e-3))))
+    t = run(nr) if nr != nr0 else t0
+    return dict(value=nr * N / t, unit=UNIT, cores=cores, kind="port",
+                sample=f"{nr} rotations x all {N} patterns of the {prob.cfg.name} workload, full "
+                       f"{s}x{s} detector ({int(prob.mask.sum())} mask pixels): one iteration "
+                       f"of the fused semantics in FP64 (oracle.fused_iteration_fp64, numpy "
+                       f"GEMMs on {cores} threads), {t:.1f} s")
+
+
+def ref_chunk_leg(prob, chunk, r0):
+    """One pass of the oracle's restatement of the reference iteration
+    (oracle.ref_iteration -> oracle/emc_oracle.c, OpenMP on all host
+    threads: int-truncated scaling denominator, FP64 per-pixel likelihood,
+    float log-sum-exp, M-step with insertion, divide, normalise) over the
+    rotation chunk [r0, r0 + chunk) x ALL patterns, full detector -- the unit
+    of work main.cpp:284-462 loops over (slice_chunk).  Returns seconds."""
+    from oracle import oracle as O
+    s = prob.cfg.side
+    q, w = prob.quats[r0:r0 + chunk], prob.weights[r0:r0 + chunk]
+    t0 = time.perf_counter()
+    O.ref_iteration(prob.init_model, prob.images, prob.mask, prob.x, prob.y, prob.z, q, w,
+                    O.sigma_at(0), s, chunk=chunk)
+    return time.perf_counter() - t0
 
 
 # ------------------------------------------------------------ GPU leg ----
@@ -619,7 +637,7 @@ def finish(args, prob, workspace, ctx, ws, rank, precision, value, ms_step, st, 
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
-        cpu, _ = cpu_leg(prob, args.cpu_seconds)
+        cpu = b1_leg(prob, args.cpu_seconds)
 
     if rank == 0:
         line = {
@@ -654,35 +672,74 @@ def finish(args, prob, workspace, ctx, ws, rank, precision, value, ms_step, st, 
 
 
 def run_reference(args):
+    """The reference arm.  The reference's own code for this path is CUDA
+    (emc_cuda.cu, emc_atomic.cu) driven by an MPI host that cannot be built
+    here; its CPU stand-in is the oracle's restatement of those kernels
+    (kind "port"), timed on a rotation chunk x all patterns per step, with
+    inputs built from the reference's own rotations.c and
+    calculate_coordinates (oracle/_ref) -- nothing of this project's library
+    is loaded.  The reference's CUDA kernels, built unchanged for sm_103a, are
+    timed beside it on one chunk (reference_gpu)."""
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    from emc_gb300 import synthetic as S
+    from emc_gb300 import synthetic as S  # data generation only: numpy / torch
+    from oracle import oracle as O
+    cfg = S.CONFIGS[args.config]
+    rotations = O.ref_rotations(cfg.rot_n)
+    coords = O.ref_coordinates(cfg.side, S.PIXEL_SIZE, S.DISTANCE, S.WAVELENGTH)
+    if rotations is None or coords is None:
+        print(json.dumps({"impl": "reference", "metric": METRIC,
+                          "unavailable": "the reference's rotations.c / emc_helper.cpp builds "
+                                         "(oracle/_ref) are missing: no reference tree staged"}),
+              flush=True)
+        return
     try:
         import torch
         dev = "cuda" if torch.cuda.is_available() else None
     except Exception:
         dev = None
-    prob = S.make_problem(S.CONFIGS[args.config], device=dev)
-    vals = []
-    info = None
-    for k in range(args.warmup + args.steps):
-        info, secs = cpu_leg(prob, max(2.0, args.cpu_seconds / max(1, args.steps)))
-        if k >= args.warmup:
-            vals.append(info["value"])
-    v = statistics.mean(vals)
+    prob = S.make_problem(cfg, device=dev, coords=coords, rotations=rotations)
     R, N = prob.quats.shape[0], prob.images.shape[0]
+    cores = os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(cores))
+    # chunk sized so that warm-up + timed steps take about args.ref_seconds
+    probe = min(R, 4)
+    t_probe = ref_chunk_leg(prob, probe, 0)
+    per_step = max(1.0, args.ref_seconds / max(1, args.warmup + args.steps))
+    chunk = int(min(R, max(1, probe * per_step / max(t_probe, 1e-3))))
+    times = []
+    for k in range(args.warmup + args.steps):
+        r0 = (k * chunk) % max(1, R - chunk + 1)
+        t = ref_chunk_leg(prob, chunk, r0)
+        if k >= args.warmup:
+            times.append(t)
+    t_step = statistics.mean(times)
+    v = chunk * N / t_step
     ref_gpu = None
     if dev == "cuda" and args.ref_gpu_chunk > 0:
         ref_gpu = ref_gpu_leg(prob, args.ref_gpu_chunk)
+    c = prob.cfg
+    sample = (f"per step: rotations [r0, r0 + {chunk}) x all {N} patterns, full {c.side}x{c.side} "
+              f"detector, one reference-semantics iteration of that chunk (oracle.ref_iteration "
+              f"-> oracle/emc_oracle.c, OpenMP, {cores} threads)")
+    workload = workload_desc(prob, "reference (quirk-exact CPU restatement)", "sequential")
+    workload["workload"] = (f"{c.name}: {c.side}^3 model, {N} patterns {c.side}x{c.side}, "
+                            f"{R} rotations (n={c.rot_n}); each step one slice_chunk of {chunk} "
+                            f"rotations x all {N} patterns (main.cpp:284-462)")
+    workload["rotation_chunk"] = chunk
+    workload["inputs"] = ("rotations from the reference's rotations.c and detector coordinates "
+                          "from its calculate_coordinates (oracle/_ref builds)")
     line = {"metric": METRIC, "impl": "reference", "value": v, "unit": UNIT, "n_gpus": ws,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": R * N / v * 1e3,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_step * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32/f64",
             "data": f"synthetic (seeded; shapes of the {args.config} configuration)",
-            "config": workload_desc(prob, "reference (quirk-exact CPU restatement)", "sequential"),
-            "cpu_baseline": {**info, "value": v},
+            "config": workload,
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": sample},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "full_iteration_ms_implied": R * N / v * 1e3,
             "reference_gpu": ref_gpu}
     print(json.dumps(line), flush=True)
 
@@ -698,9 +755,10 @@ def ref_gpu_leg(prob, chunk):
 
     import numpy as np
     import torch
+    from oracle.build import ref_dir
     env = dict(os.environ)
-    if "EMC_REF_DIR" not in env and not os.path.exists("/root/reference/emc_cuda.cu"):
-        env["EMC_REF_DIR"] = os.path.join(ROOT, "baseline", "_ref", "src")
+    if ref_dir() is not None:
+        env["EMC_REF_DIR"] = str(ref_dir())
     so = os.path.join(ROOT, "oracle", "_ref", "libemc_ref_kernels.so")
     if not os.path.exists(so):
         r = subprocess.run(["bash", os.path.join(ROOT, "oracle", "build_ref.sh"), "--kernels"],
@@ -759,8 +817,7 @@ def ref_gpu_leg(prob, chunk):
         return t
 
     one()  # warm-up (module load, first launches)
-    for _ in range(2):
-        steps.append(one())
+    steps.append(one())
     per = {k: statistics.mean(st[k] for st in steps) for k in steps[0]}
     total = sum(per.values())
     pairs = float(chunk) * N

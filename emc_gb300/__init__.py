@@ -127,8 +127,39 @@ def _close_all():
             pass
 
 
+def _stream_ordered(fn):
+    """Orders a library call against torch's current stream both ways: the
+    context's stream waits for work already queued on torch's current stream
+    (e.g. the kernel that filled an input tensor), and torch's current stream
+    waits for the library's kernels before any later torch work reads their
+    outputs.  A no-op when the two streams are the same."""
+    import functools
+
+    @functools.wraps(fn)
+    def run(self, *a, **k):
+        ctx = self if isinstance(self, Context) else self.ctx
+        if not getattr(ctx, "_h", None):
+            return fn(self, *a, **k)
+        import torch
+        cur = torch.cuda.current_stream(ctx.device)
+        handle = ctx.stream
+        if handle == cur.cuda_stream:
+            return fn(self, *a, **k)
+        mine = ctx._ext_stream(handle)
+        mine.wait_stream(cur)
+        try:
+            return fn(self, *a, **k)
+        finally:
+            cur.wait_stream(mine)
+    return run
+
+
 class Context:
-    """One device, one stream (replaces cuda_set_device, emc_cuda.cu:867-870)."""
+    """One device, one stream (replaces cuda_set_device, emc_cuda.cu:867-870).
+
+    Calls taking torch tensors are ordered against torch's current stream
+    (see _stream_ordered), so tensors written by torch before a call and read
+    by torch after it need no explicit synchronisation."""
 
     def __init__(self, device: int = 0):
         self._lib = _lib.load()
@@ -167,6 +198,15 @@ class Context:
 
     def set_stream(self, stream=None):
         self._check(self._lib.emc_set_stream(self._h, stream), "set_stream")
+
+    def _ext_stream(self, handle):
+        """torch view of the library stream `handle` (cached per handle)."""
+        import torch
+        cache = self.__dict__.setdefault("_ext_streams", {})
+        st = cache.get(handle)
+        if st is None:
+            st = cache[handle] = torch.cuda.ExternalStream(handle, device=self.device)
+        return st
 
     @property
     def stream(self) -> int:
@@ -602,3 +642,18 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+for _cls, _names in (
+        (Context, ("get_slices", "update_scaling_full", "calculate_responsabilities",
+                   "max_vector", "respons_max_expf", "norm_respons_sumexpf", "log_sum_max",
+                   "update_slices", "divide_model_by_weight", "normalize_model", "model_max",
+                   "model_average", "blur_model", "bin_images", "normalize_images", "mask_model",
+                   "model_init_radial", "model_init_orientations", "reset_real", "copy_real_d2d",
+                   "copy_real_to_host")),
+        (Plan, ("bind", "iterate", "iterate_async", "best_quaternions", "set_proposals",
+                "capture", "replay", "autotune", "time_likelihood", "set_pruning")),
+        (Proposal, ("set_data", "loss_grad", "train", "predict"))):
+    for _n in _names:
+        setattr(_cls, _n, _stream_ordered(getattr(_cls, _n)))
+del _cls, _names, _n

@@ -80,6 +80,7 @@ class Config(C.Structure):
 SIGNATURES: dict[str, tuple] = {
     "emc_ctx_create": (I, [C.POINTER(P), I]),
     "emc_ctx_destroy": (I, [P]),
+    "emc_ctx_device": (I, [P]),
     "emc_last_error": (C.c_char_p, [P]),
     "emc_set_stream": (I, [P, P]),
     "emc_get_stream": (P, [P]),

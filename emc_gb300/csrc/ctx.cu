@@ -58,6 +58,8 @@ extern "C" int emc_ctx_destroy(emc_ctx* ctx) {
   return EMC_OK;
 }
 
+extern "C" int emc_ctx_device(const emc_ctx* ctx) { return ctx ? ctx->device : -1; }
+
 extern "C" const char* emc_last_error(const emc_ctx* ctx) {
   if (!ctx) return "null context";
   return ctx->last_error.c_str();

@@ -220,11 +220,24 @@ extern "C" int emc_respons_max_expf_noalloc(const float* d_respons, const float*
     if (e) return e;
   }
   const int gx = emc::ceil_div(N_images, emc::kLseThreads);
+  // cudaLaunchKernel returns this launch's own status, so an earlier,
+  // unrelated error pending on the thread is neither reported as this call's
+  // failure nor consumed; a failed launch's error is cleared after reading.
   if (nb > 0) {
-    emc::sumexp_partial_kernel<<<dim3(gx, nb), emc::kLseThreads, 0, stream>>>(
-        d_respons, d_max, N_images, n_slices, rc, part);
-    if (cudaGetLastError() != cudaSuccess) return EMC_ERR_CUDA;
+    void* a[] = {(void*)&d_respons, (void*)&d_max, (void*)&N_images, (void*)&n_slices,
+                 (void*)&rc, (void*)&part};
+    if (cudaLaunchKernel((const void*)emc::sumexp_partial_kernel, dim3(gx, nb),
+                         dim3(emc::kLseThreads), a, 0, stream) != cudaSuccess) {
+      cudaGetLastError();
+      return EMC_ERR_CUDA;
+    }
   }
-  emc::sum_final_kernel<<<gx, emc::kLseThreads, 0, stream>>>(part, N_images, nb, d_sum);
-  return cudaGetLastError() == cudaSuccess ? EMC_OK : EMC_ERR_CUDA;
+  const float* cpart = part;
+  void* b[] = {(void*)&cpart, (void*)&N_images, (void*)&nb, (void*)&d_sum};
+  if (cudaLaunchKernel((const void*)emc::sum_final_kernel, dim3(gx), dim3(emc::kLseThreads), b, 0,
+                       stream) != cudaSuccess) {
+    cudaGetLastError();
+    return EMC_ERR_CUDA;
+  }
+  return EMC_OK;
 }

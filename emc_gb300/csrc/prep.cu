@@ -114,21 +114,24 @@ __host__ __device__ inline double centre_radius3(int x, int y, int z, int side) 
 }
 
 // model = radavg[r] (1 - (rad - r)) + radavg[r+1] (rad - r) for r = (int)rad
-// < side/2, else -1.  radavg has side/2 + 1 entries; the last is 0 (the
-// reference reads one past its array there).
+// < side/2, else -1, with the reference's types (emc_helper.cpp:487-496): rad
+// is a float (the double root rounded), rad - r a float difference, the first
+// product double (1.0 is a double literal), the second a float product.
+// radavg has side/2 + 1 entries; the last is 0 (the reference reads one past
+// its array there).
 __global__ void radial_model_kernel(const float* __restrict__ radavg, int side,
                                     float* __restrict__ model) {
   const long long n3 = (long long)side * side * side;
   const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= n3) return;
   const int x = (int)(v % side), y = (int)((v / side) % side), z = (int)(v / ((long long)side * side));
-  const double rad = centre_radius3(x, y, z, side);
+  const float rad = (float)centre_radius3(x, y, z, side);
   const int r = (int)rad;
   float out = -1.0f;
   if ((double)r < (double)side / 2.0) {
-    const double f = __dsub_rn(rad, (double)r);
-    out = (float)__dadd_rn(__dmul_rn((double)radavg[r], __dsub_rn(1.0, f)),
-                           __dmul_rn((double)radavg[r + 1], f));
+    const float f = __fsub_rn(rad, (float)r);
+    out = (float)__dadd_rn(__dmul_rn((double)radavg[r], __dsub_rn(1.0, (double)f)),
+                           (double)__fmul_rn(radavg[r + 1], f));
   }
   model[v] = out;
 }

@@ -70,6 +70,9 @@ typedef struct emc_plan emc_plan;
 int emc_ctx_create(emc_ctx** out, int device);
 /* Destroy every plan and batch of a context before the context. */
 int emc_ctx_destroy(emc_ctx* ctx);
+/* The device the context was created on (cuda_get_device, emc_cuda.cu:861-865,
+ * for a caller whose current device may have changed since); -1 for NULL. */
+int emc_ctx_device(const emc_ctx* ctx);
 /* Text of the last error on this context (never NULL). */
 const char* emc_last_error(const emc_ctx* ctx);
 /* Use an external cudaStream_t (NULL: the context's own stream). */
@@ -178,7 +181,11 @@ int emc_norm_respons_sumexpf(emc_ctx* ctx, float* d_respons, const float* d_sum,
  * N_images may not exceed EMC_NOALLOC_PARTIALS (EMC_ERR_INVALID otherwise).
  * The first call on each device looks up the array's device address
  * (cudaGetSymbolAddress, no allocation) and should come before any stream
- * capture.  Calls that overlap on the GPU share the array and race. */
+ * capture.  That address is cached per device for the life of the process:
+ * after cudaDeviceReset on a device it is stale, so a process that resets a
+ * device must not call this entry point on it again.  Calls that overlap on
+ * the GPU share the array and race.  Returns EMC_ERR_CUDA only for this
+ * call's own launches; an earlier error pending on the thread is left as is. */
 #define EMC_NOALLOC_PARTIALS (1 << 20)
 int emc_respons_max_expf_noalloc(const float* d_respons, const float* d_max, int N_images,
                                  int n_slices, float* d_sum, void* cuda_stream);

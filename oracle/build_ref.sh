@@ -5,27 +5,30 @@
 #   oracle/_ref/libemc_ref_kernels.so  emc_cuda.cu + emc_atomic.cu for sm_103a,
 #                                      behind the C wrappers of ref_harness.cu
 #                                      (only with --kernels; needs nvcc)
-# The reference tree is $EMC_REF_DIR, else /root/reference, else the staged
-# copy baseline/_ref/src (git-ignored; see --stage).  Outputs go to
-# oracle/_ref/ only.
-#   --stage   copy the reference files the kernels need into baseline/_ref/src
-#             (git-ignored) so that a GPU machine without the reference tree can
-#             build the kernel harness.
+#   oracle/_ref/libemc_ref_helper.so   emc_helper.cpp + rotations.c (host) behind
+#                                      the C wrappers of ref_helper_harness.cpp
+#                                      (only with --helper)
+# The reference tree is $EMC_REF_DIR, else the staged copy baseline/_ref/src
+# (git-ignored; see --stage).  Outputs go to oracle/_ref/ only.
+#   --stage   copy the reference files the checkers need from $EMC_REF_DIR into
+#             baseline/_ref/src (git-ignored) so that a machine without the
+#             reference tree (the GPU host) can build them too.
 set -euo pipefail
 here="$(cd "$(dirname "$0")" && pwd)"
 repo="$(cd "$here/.." && pwd)"
 out="$here/_ref"
-ref="${EMC_REF_DIR:-}"
-if [[ -z "$ref" ]]; then
-  if [[ -d /root/reference ]]; then ref=/root/reference; else ref="$repo/baseline/_ref/src"; fi
-fi
+ref="${EMC_REF_DIR:-$repo/baseline/_ref/src}"
 want_kernels=0
+want_helper=0
 for a in "$@"; do
   case "$a" in
     --kernels) want_kernels=1 ;;
+    --helper) want_helper=1 ;;
     --stage)
       mkdir -p "$repo/baseline/_ref/src"
-      for f in rotations.c rotations.h emc_cuda.cu emc_atomic.cu emc_cuda_help.h emc_helper.h configs.h; do
+      if [[ "$ref" == "$repo/baseline/_ref/src" ]]; then echo "--stage needs EMC_REF_DIR" >&2; exit 1; fi
+      for f in rotations.c rotations.h emc_cuda.cu emc_atomic.cu emc_cuda_help.h emc_helper.h \
+               emc_helper.cpp configs.h emc.conf; do
         cp "$ref/$f" "$repo/baseline/_ref/src/$f"
       done
       echo "staged reference sources in baseline/_ref/src"
@@ -41,6 +44,16 @@ gcc -O2 -std=gnu99 -w -I"$here/shim" -I"$ref" -include stdio.h -include stdlib.h
     -include string.h -include math.h \
     "$ref/rotations.c" "$here/ref_rotations_main.c" "$here/shim/spimage_stubs.c" -lm \
     -o "$out/ref_rotations"
+if [[ $want_helper == 1 ]]; then
+  # float arithmetic without contraction, as the reference's x86-64 build
+  # (no FMA in its default target) evaluates it, on every host
+  gcc -O2 -std=gnu99 -fPIC -w -ffp-contract=off -I"$here/shim" -I"$ref" -include stdio.h \
+      -include stdlib.h -include string.h -include math.h -c "$ref/rotations.c" \
+      -o "$out/rotations_helper.o"
+  g++ -O2 -std=c++17 -fPIC -w -ffp-contract=off -I"$here/shim" -I"$ref" -include cstdio \
+      -include cstring -shared "$ref/emc_helper.cpp" "$here/ref_helper_harness.cpp" \
+      "$out/rotations_helper.o" -o "$out/libemc_ref_helper.so"
+fi
 if [[ $want_kernels == 1 ]]; then
   # emc_cuda.cu and emc_atomic.cu each define inblock_reduce, so they are
   # separate translation units, as in the reference's own build.

@@ -464,13 +464,17 @@ void oracle_model_init_radial(const float* images, int n, int side, int float_su
       for (int z = 0; z < side; ++z) {
         const double dx = (double)(float)x - h + 0.5, dy = (double)(float)y - h + 0.5,
                      dz = (double)(float)z - h + 0.5;
-        const double rad = sqrt(dx * dx + dy * dy + dz * dz);
+        /* `real rad` in the reference (emc_helper.cpp:487): the double root
+           rounded to float; rad - r is a float difference, the first product
+           double (1.0 is a double literal), the second a float product */
+        const float rad = (float)sqrt(dx * dx + dy * dy + dz * dz);
         const int r = (int)rad;
         const size_t v = ((size_t)z * side + y) * side + x;
-        if (r < h)
-          model[v] = (float)(radavg[r] * (1.0 - (rad - (double)r)) +
-                             radavg[r + 1] * (rad - (double)r));
-        else
+        if (r < h) {
+          const float f = rad - (float)r;
+          const float hi = radavg[r + 1] * f;
+          model[v] = (float)((double)radavg[r] * (1.0 - (double)f) + (double)hi);
+        } else
           model[v] = -1.0f;
       }
   if (radavg_out) memcpy(radavg_out, radavg, sizeof(float) * ((size_t)nr + 1));

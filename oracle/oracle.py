@@ -394,3 +394,37 @@ def model_init_orientations(images, mask, side, quats, x, y, z):
     lib().oracle_model_init_orientations(images, _i(mask), images.shape[0], side, _f(quats),
                                          _f(x), _f(y), _f(z), model, weight)
     return model, weight
+
+
+# ------------------------------------- the reference's own host code ----
+def ref_rotations(n):
+    """(quats [R, 4], weights [R]) float32 from the reference's own
+    generate_rotation_list (rotations.c:77-458, oracle/_ref/ref_rotations
+    built by build_ref.sh), or None when that build is absent."""
+    import subprocess
+    import tempfile
+    exe = HERE / "_ref" / "ref_rotations"
+    if not exe.exists():
+        return None
+    with tempfile.TemporaryDirectory() as d:  # it also writes debug_samples.data there
+        subprocess.run([str(exe), str(int(n)), f"{d}/rot.bin"], cwd=d, check=True,
+                       capture_output=True)
+        b = open(f"{d}/rot.bin", "rb").read()
+    R = int(np.frombuffer(b[:4], np.int32)[0])
+    q = np.frombuffer(b[4:4 + 16 * R], np.float32).reshape(R, 4).copy()
+    w = np.frombuffer(b[4 + 16 * R:4 + 20 * R], np.float32).copy()
+    return q, w
+
+
+def ref_coordinates(side, pixel_size, detector_distance, wavelength):
+    """(x, y, z) float32 [side*side] from the reference's own
+    calculate_coordinates (emc_helper.cpp:55-79 behind
+    oracle/ref_helper_harness.cpp), or None when that build is absent."""
+    from .build import ref_helper
+    h = ref_helper()
+    if h is None:
+        return None
+    out = [np.zeros(side * side, np.float32) for _ in range(3)]
+    h.refh_calculate_coordinates(side, pixel_size, detector_distance, wavelength,
+                                 *[a.ctypes.data_as(C.c_void_p) for a in out])
+    return tuple(out)

@@ -2,8 +2,8 @@
 
 Runs on a machine with a GB300.  Builds oracle/_ref/libemc_ref_kernels.so
 from the reference sources (emc_cuda.cu, emc_atomic.cu compiled unchanged for
-sm_103a behind oracle/ref_harness.cu) -- from $EMC_REF_DIR, else the reference
-tree, else the staged copy in baseline/_ref/src -- feeds it a small seeded
+sm_103a behind oracle/ref_harness.cu) -- from $EMC_REF_DIR, else the
+staged copy in baseline/_ref/src -- feeds it a small seeded
 problem and writes inputs and outputs to the file given as the argument
 (default ref_kernels_golden.npz in the working directory), which is committed
 as tests/golden/ref_kernels_golden.npz.
@@ -28,9 +28,11 @@ def main():
 
     from emc_gb300 import synthetic as S
 
+    from oracle.build import ref_dir
     env = dict(os.environ)
-    if "EMC_REF_DIR" not in env and not Path("/root/reference/emc_cuda.cu").exists():
-        env["EMC_REF_DIR"] = str(ROOT / "baseline" / "_ref" / "src")
+    if ref_dir() is None:
+        raise SystemExit("no reference tree: set EMC_REF_DIR or stage it (build_ref.sh --stage)")
+    env["EMC_REF_DIR"] = str(ref_dir())
     subprocess.run(["bash", str(ROOT / "oracle" / "build_ref.sh"), "--kernels"], check=True, env=env)
     lib = C.CDLL(str(ROOT / "oracle" / "_ref" / "libemc_ref_kernels.so"))
     lib.ref_model_average.restype = C.c_float

@@ -66,8 +66,10 @@ def test_diff_types(built):
 
 
 def test_reference_emc_conf_if_present(built):
-    path = os.environ.get("EMC_REF_DIR", "/root/reference") + "/emc.conf"
-    if not os.path.exists(path):
+    from oracle.build import ref_dir
+    ref = ref_dir()
+    path = os.path.join(str(ref), "emc.conf") if ref else ""
+    if not path or not os.path.exists(path):
         pytest.skip("reference tree not present")
     c = E.read_config(path)
     assert c.model_side == 64 and c.rotations_n == 12 and c.diff == E.DIFF_POISSON

@@ -34,6 +34,8 @@ def test_noalloc_matches_allocating_entry_point(ctx, cuda, N, R):
     stream = torch.cuda.Stream(cuda)
     for _ in range(2):
         got = torch.full((N,), -7.0, device=cuda)
+        # the fill above runs on torch's current stream: the side stream waits for it
+        stream.wait_stream(torch.cuda.current_stream(cuda))
         rc = lib.emc_respons_max_expf_noalloc(L.data_ptr(), mx.data_ptr(), N, R, got.data_ptr(),
                                               stream.cuda_stream)
         assert rc == 0

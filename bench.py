@@ -69,6 +69,8 @@ def parse():
                          "the large configuration, 0 otherwise)")
     ap.add_argument("--estep-pair", type=int, choices=[0, 1], default=1,
                     help="tensor path: full likelihood scans on CTA pairs (EMC_OPT_ESTEP_PAIR)")
+    ap.add_argument("--mstep-pair", type=int, choices=[0, 1], default=1,
+                    help="tensor path: full-scan M-step on CTA pairs (EMC_OPT_MSTEP_PAIR)")
     ap.add_argument("--raster", type=int, default=0,
                     help="tensor path: the likelihood kernel's tile order (EMC_OPT_ESTEP_RASTER); "
                          "0 (default): chosen by emc_plan_autotune before the warm-up")
@@ -303,6 +305,7 @@ def run_ours(args):
         if prec == E.PREC_MIXED and args.counts_round:
             p.set_option(E.Plan.OPT_COUNTS_ROUND, 1)
         p.set_option(E.Plan.OPT_ESTEP_PAIR, args.estep_pair)
+        p.set_option(E.Plan.OPT_MSTEP_PAIR, args.mstep_pair)
         p.bind(images, mask, x, y, z, rot, w)
         return p
 
@@ -654,6 +657,8 @@ def finish(args, prob, workspace, ctx, ws, rank, precision, value, ms_step, st, 
                                      0: "G, H fp16 hi"}[args.estep_ghlo],
                            mstep_atomics="warp-aggregated" if args.mstep_aggregate else "per pair",
                            estep_kernel="CTA pairs (256-row MMAs)" if args.estep_pair
+                           else "single CTAs",
+                           mstep_kernel="CTA pairs (256-row MMAs)" if args.mstep_pair
                            else "single CTAs",
                            counts="counts above 2048 rounded to fp16" if
                            (args.counts_round and precision == "mixed") else "exact"),

@@ -454,6 +454,8 @@ class Plan:
     OPT_ESTEP_RASTER = 6
     OPT_ESTEP_PAIR = 7
     OPT_MSTEP_RASTER = 8
+    OPT_DEBUG_SPIN = 9
+    OPT_MSTEP_PAIR = 10
 
     def set_option(self, option: int, value: int):
         self.ctx._check(self._lib.emc_plan_set_option(self._h, option, value), "plan_set_option")
@@ -490,6 +492,31 @@ class Plan:
         out = (C.c_float * 6)()
         self.ctx._check(self._lib.emc_plan_phase_ms(self._h, out, 6), "plan_phase_ms")
         return dict(zip(self.PHASES, [float(v) for v in out]))
+
+    # -- one rank of a rotation split (emc_rank_*) ----------------------------
+    def rank_estep(self, model, sigma, d_max, d_sumexp):
+        """Expand + likelihood over this plan's rotations; d_max [N] float32
+        and d_sumexp [N] float64 receive the per-pattern partials."""
+        import torch
+        self.ctx._check(self._lib.emc_rank_estep(
+            self._h, _ptr(model, torch.float32, "model"), float(sigma),
+            _ptr(d_max, torch.float32, "d_max"), _ptr(d_sumexp, torch.float64, "d_sumexp")),
+            "rank_estep")
+
+    def rank_mstep(self, lse, model_sum, weight_sum):
+        """M-step of this plan's rotations with the global lse [N] float64;
+        writes the un-normalised sums."""
+        import torch
+        self.ctx._check(self._lib.emc_rank_mstep(
+            self._h, _ptr(lse, torch.float64, "lse"), _ptr(model_sum, torch.float32, "model_sum"),
+            _ptr(weight_sum, torch.float32, "weight_sum")), "rank_mstep")
+
+    def model_from_sums(self, model_sum, weight_sum, n_ranks, model, weight):
+        import torch
+        self.ctx._check(self._lib.emc_model_from_sums(
+            self._h, _ptr(model_sum, torch.float32), _ptr(weight_sum, torch.float32),
+            int(n_ranks), _ptr(model, torch.float32, "model"),
+            _ptr(weight, torch.float32, "weight")), "model_from_sums")
 
     def results(self):
         r, s, l = C.c_void_p(), C.c_void_p(), C.c_void_p()
@@ -652,7 +679,8 @@ for _cls, _names in (
                    "model_init_radial", "model_init_orientations", "reset_real", "copy_real_d2d",
                    "copy_real_to_host")),
         (Plan, ("bind", "iterate", "iterate_async", "best_quaternions", "set_proposals",
-                "capture", "replay", "autotune", "time_likelihood", "set_pruning")),
+                "capture", "replay", "autotune", "time_likelihood", "set_pruning", "results",
+                "rank_estep", "rank_mstep", "model_from_sums")),
         (Proposal, ("set_data", "loss_grad", "train", "predict"))):
     for _n in _names:
         setattr(_cls, _n, _stream_ordered(getattr(_cls, _n)))

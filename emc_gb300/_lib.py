@@ -151,6 +151,9 @@ SIGNATURES: dict[str, tuple] = {
     "emc_batch_wait": (I, [P, P]),
     "emc_batch_destroy": (I, [P]),
     "emc_plan_results": (I, [P, C.POINTER(P), C.POINTER(P), C.POINTER(P)]),
+    "emc_rank_estep": (I, [P, P, F, P, P]),
+    "emc_rank_mstep": (I, [P, P, P, P]),
+    "emc_model_from_sums": (I, [P, P, P, I, P, P]),
     "emc_plan_set_profiling": (I, [P, I]),
     "emc_plan_set_option": (I, [P, I, I]),
     "emc_plan_autotune": (I, [P, P, F, C.POINTER(I), C.POINTER(F)]),

@@ -654,7 +654,7 @@ __global__ void __launch_bounds__(kMprepThreads) mprep_kernel(
     float* __restrict__ Q, __half* __restrict__ Qh, __half* __restrict__ Ql,
     float* __restrict__ qscale, int ldq, float* __restrict__ T, double* __restrict__ row_mass,
     double* __restrict__ row_bound, int stage, const unsigned char* __restrict__ tstate,
-    int n_rt, double* __restrict__ row_margin) {
+    int n_rt, double* __restrict__ row_margin, int write_p) {
   extern __shared__ float qrow[];  // [N] when stage: the row's P c_i / phi
   const int r = blockIdx.x;
   // pruned iteration: tstate[pattern tile][rotation tile] = 0 not evaluated
@@ -700,7 +700,7 @@ __global__ void __launch_bounds__(kMprepThreads) mprep_kernel(
       P.y = elem(i + 1, st, l.y, f.y, make_float2(s01.z, s01.w), ks.y, cn.y);
       P.z = elem(i + 2, st, l.z, f.z, make_float2(s23.x, s23.y), ks.z, cn.z);
       P.w = elem(i + 3, st, l.w, f.w, make_float2(s23.z, s23.w), ks.w, cn.w);
-      L4[j] = P;
+      if (write_p) L4[j] = P;
     }
   } else {
     for (int i = threadIdx.x; i < N; i += blockDim.x) {
@@ -708,7 +708,8 @@ __global__ void __launch_bounds__(kMprepThreads) mprep_kernel(
       const int st = ts ? ts[(size_t)(i >> 7) * n_rt] : 1;
       const float l = L[e];
       const float f = st ? PHI[e] : 0.0f;
-      L[e] = elem(i, st, l, f, lse2[i], __ldg(Ksum + i), __ldg(cnorm + i));
+      const float P = elem(i, st, l, f, lse2[i], __ldg(Ksum + i), __ldg(cnorm + i));
+      if (write_p) L[e] = P;
     }
   }
   if (Q)
@@ -764,6 +765,32 @@ __global__ void __launch_bounds__(kMprepThreads) mprep_kernel(
     if (Ql) *reinterpret_cast<uint2*>(Ql + (size_t)r * ldq + i) = lo.u;
   }
   if (threadIdx.x == 0) qscale[r] = ldexpf(1.0f, -ex);
+}
+
+// P = exp(L - lse) in place over the plan's [R][N] rows, with mprep's own
+// expression for an evaluated pair (bit-identical to an eagerly written P).
+__global__ void respons_from_loglik_kernel(float* __restrict__ L, const float2* __restrict__ lse2,
+                                           int N, long long total) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += stride) {
+    const int i = (int)(e % N);
+    const float l = L[e];
+    const float2 li = lse2[i];
+    float P = 0.0f;
+    if (isfinite(li.x) && l > -INFINITY) P = expf((l - li.x) - li.y);
+    L[e] = P;
+  }
+}
+
+int plan_respons_ready(emc_plan* p) {
+  if (p->p_written) return EMC_OK;
+  emc_ctx* ctx = p->ctx;
+  const long long total = (long long)p->d.n_rot * p->d.n_images;
+  respons_from_loglik_kernel<<<ctx->sm_count * 8, 256, 0, ctx->stream>>>(p->L, p->lse2,
+                                                                        p->d.n_images, total);
+  const int rc = after_launch(ctx, "respons_from_loglik_kernel");
+  if (!rc) p->p_written = true;
+  return rc;
 }
 
 // ---------------------------------------------------------- insert -------
@@ -965,6 +992,72 @@ __global__ void finish_insert_kernel(const unsigned long long* __restrict__ fm,
       m = a.x;
       w = a.y;
     }
+    weight[v] = w;
+    model[v] = w > 0.0f ? __fdiv_rn(m, w) : -1.0f;
+  }
+}
+
+// ---- one rank of a rotation split --------------------------------------
+// Per pattern, over this plan's rotations: the largest log-likelihood and the
+// sum of exp(L - max) (FP64), from the per-tile partials.
+__global__ void rank_partial_kernel(const float2* __restrict__ part, int n_rt, int N,
+                                    float* __restrict__ out_max, double* __restrict__ out_sum) {
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= N) return;
+  float M = -INFINITY;
+  for (int t = 0; t < n_rt; ++t) M = fmaxf(M, part[(size_t)t * N + n].x);
+  double sum = 0.0;
+  if (M > -INFINITY)
+    for (int t = 0; t < n_rt; ++t) {
+      const float2 v = part[(size_t)t * N + n];
+      if (v.x > -INFINITY) sum += (double)v.y * exp((double)v.x - (double)M);
+    }
+  out_max[n] = M;
+  out_sum[n] = sum;
+}
+
+// The normaliser combined over all ranks, in the plan's own form (FP64 and
+// float hi + lo).
+__global__ void lse_from_global_kernel(const double* __restrict__ lse_in, int N,
+                                       double* __restrict__ lse, float2* __restrict__ lse2) {
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= N) return;
+  const double l = lse_in[n];
+  lse[n] = l;
+  const float hi = (float)l;
+  lse2[n] = make_float2(hi, isfinite(l) ? (float)(l - (double)hi) : 0.0f);
+}
+
+// The inserted sums as floats (model sum of T_r x slice, weight sum of T_r),
+// exactly as finish_insert_kernel reads them.
+__global__ void sums_out_kernel(const unsigned long long* __restrict__ fm,
+                                const unsigned long long* __restrict__ fw,
+                                const double* __restrict__ bounds, const float2* __restrict__ acc2,
+                                float* __restrict__ msum, float* __restrict__ wsum, long long n) {
+  const double inv_m = fm ? 1.0 / fixed_scale(bounds[0]) : 0.0;
+  const double inv_w = fm ? 1.0 / fixed_scale(bounds[1]) : 0.0;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += stride) {
+    if (fm) {
+      msum[v] = (float)((double)(long long)fm[v] * inv_m);
+      wsum[v] = (float)((double)(long long)fw[v] * inv_w);
+    } else {
+      const float2 a = acc2[v];
+      msum[v] = a.x;
+      wsum[v] = a.y;
+    }
+  }
+}
+
+// main.cpp:467-476 after the all-reduce: both sums divided by the number of
+// ranks (devide_part), then model / weight (-1 where the weight is 0).
+__global__ void model_from_sums_kernel(const float* __restrict__ msum,
+                                       const float* __restrict__ wsum, float n_ranks,
+                                       float* __restrict__ model, float* __restrict__ weight,
+                                       long long n) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += stride) {
+    const float m = __fdiv_rn(msum[v], n_ranks), w = __fdiv_rn(wsum[v], n_ranks);
     weight[v] = w;
     model[v] = w > 0.0f ? __fdiv_rn(m, w) : -1.0f;
   }
@@ -1276,55 +1369,80 @@ static int plan_mstep_fp32(emc_plan* p, float* model, float* weight, const Inser
   return after_launch(ctx, "mstep_fp32_kernel");
 }
 
-// Enqueues one iteration on the context stream: kernels, device-to-device
-// copies and memsets only (no allocation, no host copy, no synchronisation),
-// so the sequence can be captured in a CUDA graph.  The E-step reads sigma
-// from p->sigma_dev.
-static int iterate_enqueue(emc_plan* p, float* d_model, float* d_weight) {
+// The stages of one iteration, each enqueued on the context stream: kernels,
+// device-to-device copies and memsets only (no allocation, no host copy, no
+// synchronisation), so the sequence can be captured in a CUDA graph.  The
+// E-step reads sigma from p->sigma_dev.  A full iteration runs them in order;
+// one rank of a rotation split (emc_rank_*) runs the E-step, exports its
+// per-pattern partials, and resumes at the M-step with the global normaliser.
+static int enqueue_normalise(emc_plan* p, float* d_model);
+
+static int mark_phase(emc_plan* p, int i) {
   emc_ctx* ctx = p->ctx;
-  const int R = p->d.n_rot, N = p->d.n_images;
-  const long long n3 = (long long)p->d.side * p->d.side * p->d.side;
+  if (p->profiling) EMC_CUDA(ctx, cudaEventRecord(p->ev[i], ctx->stream));
+  return EMC_OK;
+}
+
+// expand + scaling + likelihood + per-tile (max, sum exp) partials
+static int enqueue_estep(emc_plan* p, float* d_model) {
+  emc_ctx* ctx = p->ctx;
+  const int N = p->d.n_images;
   int rc;
-  auto mark = [&](int i) -> int {
-    if (p->profiling) EMC_CUDA(ctx, cudaEventRecord(p->ev[i], ctx->stream));
-    return EMC_OK;
-  };
-  if ((rc = mark(0))) return rc;
+  if ((rc = mark_phase(p, 0))) return rc;
   EMC_CUDA(ctx, cudaMemsetAsync(p->flags + 4, 0, sizeof(int), ctx->stream));
   if (p->prune_tiles) {  // skipped tiles contribute (max, sum exp) = (-inf, 0)
     fill_part_kernel<<<ctx->sm_count * 4, 256, 0, ctx->stream>>>(p->part,
                                                                 (size_t)p->n_rt * N);
     if ((rc = after_launch(ctx, "fill_part_kernel"))) return rc;
   }
-  // expand
   if ((rc = plan_expand(p, d_model))) return rc;
-  if ((rc = mark(1))) return rc;
-  // scaling + likelihood + per-tile LSE partials
+  if ((rc = mark_phase(p, 1))) return rc;
   if (p->d.precision == EMC_PREC_MIXED)
     rc = tc_estep(p);
   else
     rc = plan_estep_fp32(p);
   if (rc) return rc;
-  if ((rc = mark(2))) return rc;
-  // normaliser
+  return mark_phase(p, 2);
+}
+
+// the normaliser lse_i from the per-tile partials, and the total log-likelihood
+static int enqueue_lse(emc_plan* p) {
+  emc_ctx* ctx = p->ctx;
+  const int N = p->d.n_images;
+  int rc;
   lse_combine_kernel<<<ceil_div(N, 256), 256, 0, ctx->stream>>>(p->part, p->n_rt, N, p->lse,
                                                                 p->lse2);
   if ((rc = after_launch(ctx, "lse_combine_kernel"))) return rc;
   finite_sum_kernel<<<1, 256, 0, ctx->stream>>>(p->lse, N, p->red + kRedLL);
   if ((rc = after_launch(ctx, "finite_sum_kernel"))) return rc;
-  if ((rc = mark(3))) return rc;
+  return mark_phase(p, 3);
+}
+
+// responsibilities (mprep) and the M-step with insertion into the zeroed
+// accumulators (acc2, or fix_m / fix_w when deterministic); model / weight
+// are the buffers the insertion context names (not written here)
+static int enqueue_mstep(emc_plan* p, float* d_model, float* d_weight) {
+  emc_ctx* ctx = p->ctx;
+  const int R = p->d.n_rot, N = p->d.n_images;
+  const long long n3 = (long long)p->d.side * p->d.side * p->d.side;
+  int rc;
   double* row_mass = p->red + kRedSlots;
   double* row_bound = row_mass + p->Rp;
   const bool tcm = p->d.precision == EMC_PREC_MIXED;
   const int stage = tcm && N <= kMprepStageMax;
+  // P is written over L only where it is read back: by the pruning of the
+  // next iteration, or by mprep's own second pass when the row of Q does not
+  // fit shared memory.  Otherwise the responsibilities are formed on request
+  // (emc_plan_results, emc_plan_best_quaternions: plan_respons_ready).
+  const int write_p = (p->prune != nullptr || (tcm && !stage)) ? 1 : 0;
   mprep_kernel<<<R, kMprepThreads, stage ? sizeof(float) * N : 0, ctx->stream>>>(
       p->L, p->PHI, p->lse2, p->Ksum, p->cnorm, R, N, tcm ? nullptr : p->Q,
       tcm ? p->Qh : nullptr, tcm && p->mstep_q_lo ? p->Ql : nullptr, p->qscale, p->Np, p->T,
       row_mass, row_bound,
-      stage, p->prune_tiles ? p->prune_state : nullptr, p->n_rt, p->prune_margin);
+      stage, p->prune_tiles ? p->prune_state : nullptr, p->n_rt, p->prune_margin, write_p);
+  p->p_written = write_p != 0;
   if ((rc = after_launch(ctx, "mprep_kernel"))) return rc;
-  if ((rc = mark(4))) return rc;
-  // M-step into zeroed accumulators
+  if ((rc = mark_phase(p, 4))) return rc;
   const bool det = p->d.insert_mode == EMC_INSERT_DETERMINISTIC;
   if (det) {
     insert_bounds_kernel<<<1, 256, 0, ctx->stream>>>(row_mass, row_bound, R, p->P_eff,
@@ -1336,19 +1454,35 @@ static int iterate_enqueue(emc_plan* p, float* d_model, float* d_weight) {
     EMC_CUDA(ctx, cudaMemsetAsync(p->acc2, 0, sizeof(float2) * n3, ctx->stream));
   }
   InsertCtx ins = make_insert_ctx(p, d_model, d_weight);
-  if (p->d.precision == EMC_PREC_MIXED)
+  if (tcm)
     rc = tc_mstep(p, d_model, d_weight);
   else
     rc = plan_mstep_fp32(p, d_model, d_weight, ins);
-  if (rc) return rc;
+  return rc;
+}
+
+// model = inserted sums / weight, normalised to a positive mean of 1, blurred
+static int enqueue_finish(emc_plan* p, float* d_model, float* d_weight) {
+  emc_ctx* ctx = p->ctx;
+  const long long n3 = (long long)p->d.side * p->d.side * p->d.side;
+  const bool det = p->d.insert_mode == EMC_INSERT_DETERMINISTIC;
+  int rc;
   {
     const int nb = (int)std::min<long long>(ceil_div(n3, 256), (long long)ctx->sm_count * 8);
-    finish_insert_kernel<<<nb, 256, 0, ctx->stream>>>(det ? p->fix_m : nullptr, p->fix_w, ins.bounds,
-                                                       p->acc2, d_model, d_weight, n3);
+    finish_insert_kernel<<<nb, 256, 0, ctx->stream>>>(det ? p->fix_m : nullptr, p->fix_w,
+                                                       p->red + kRedBoundM, p->acc2, d_model,
+                                                       d_weight, n3);
     if ((rc = after_launch(ctx, "finish_insert_kernel"))) return rc;
   }
-  if ((rc = mark(5))) return rc;
-  // normalise, blur
+  if ((rc = mark_phase(p, 5))) return rc;
+  return enqueue_normalise(p, d_model);
+}
+
+// model / positive mean (the reference's normalize_model), then the blur
+static int enqueue_normalise(emc_plan* p, float* d_model) {
+  emc_ctx* ctx = p->ctx;
+  const long long n3 = (long long)p->d.side * p->d.side * p->d.side;
+  int rc;
   double* mean_stats = p->red + kRedMean;
   // launch_positive_mean writes {sum, count} then its partials after them;
   // kRedMean + 2 + 2*1024 fits in the reduction buffer tail.
@@ -1360,7 +1494,15 @@ static int iterate_enqueue(emc_plan* p, float* d_model, float* d_weight) {
   if (p->d.blur_sigma > 0.0f) {
     if ((rc = blur_run(ctx, d_model, p->blur))) return rc;
   }
-  return mark(6);
+  return mark_phase(p, 6);
+}
+
+static int iterate_enqueue(emc_plan* p, float* d_model, float* d_weight) {
+  int rc;
+  if ((rc = enqueue_estep(p, d_model))) return rc;
+  if ((rc = enqueue_lse(p))) return rc;
+  if ((rc = enqueue_mstep(p, d_model, d_weight))) return rc;
+  return enqueue_finish(p, d_model, d_weight);
 }
 
 static int set_sigma(emc_plan* p, float sigma) {
@@ -1583,6 +1725,16 @@ extern "C" int emc_plan_set_option(emc_plan* p, int option, int value) {
     p->estep_pair = value;
     return EMC_OK;
   }
+  if (option == EMC_OPT_MSTEP_PAIR) {
+    EMC_REQUIRE(ctx, value == 0 || value == 1, "plan_set_option: M-step pair %d", value);
+    p->mstep_pair = value;
+    return EMC_OK;
+  }
+  if (option == EMC_OPT_DEBUG_SPIN) {
+    EMC_REQUIRE(ctx, value >= 0, "plan_set_option: debug spin %d", value);
+    p->debug_spin = (unsigned)value;
+    return EMC_OK;
+  }
   if (option == EMC_OPT_MSTEP_AGGREGATE) {
     EMC_REQUIRE(ctx, value == 0 || value == 1, "plan_set_option: aggregate %d", value);
     p->mstep_aggregate = value;
@@ -1665,8 +1817,70 @@ extern "C" int emc_plan_phase_ms(emc_plan* p, float* ms, int n) {
 extern "C" int emc_plan_results(emc_plan* p, const float** d_respons, const float** d_scaling,
                                 const double** d_lse) {
   if (!p) return EMC_ERR_INVALID;
+  if (d_respons) {
+    const int rc = plan_respons_ready(p);
+    if (rc) return rc;
+  }
   if (d_respons) *d_respons = p->L;
   if (d_scaling) *d_scaling = p->PHI;
   if (d_lse) *d_lse = p->lse;
   return EMC_OK;
+}
+
+// ---- one rank of the reference's rotation split (main.cpp:141-154) -------
+extern "C" int emc_rank_estep(emc_plan* p, float* d_model, float sigma, float* d_max,
+                              double* d_sumexp) {
+  if (!p) return EMC_ERR_INVALID;
+  emc_ctx* ctx = p->ctx;
+  EMC_REQUIRE(ctx, p->bound, "rank_estep: plan not bound");
+  EMC_REQUIRE(ctx, d_model && d_max && d_sumexp, "rank_estep: null argument");
+  EMC_REQUIRE(ctx, !p->prune, "rank_estep: pruning is not supported on a rotation split");
+  int rc = set_sigma(p, sigma);
+  if (rc) return rc;
+  if ((rc = enqueue_estep(p, d_model))) return rc;
+  const int N = p->d.n_images;
+  rank_partial_kernel<<<ceil_div(N, 256), 256, 0, ctx->stream>>>(p->part, p->n_rt, N, d_max,
+                                                                 d_sumexp);
+  return after_launch(ctx, "rank_partial_kernel");
+}
+
+extern "C" int emc_rank_mstep(emc_plan* p, const double* d_lse, float* d_model_sum,
+                              float* d_weight_sum) {
+  if (!p) return EMC_ERR_INVALID;
+  emc_ctx* ctx = p->ctx;
+  EMC_REQUIRE(ctx, p->bound, "rank_mstep: plan not bound");
+  EMC_REQUIRE(ctx, d_lse && d_model_sum && d_weight_sum, "rank_mstep: null argument");
+  EMC_REQUIRE(ctx, !p->prune, "rank_mstep: pruning is not supported on a rotation split");
+  const int N = p->d.n_images;
+  const long long n3 = (long long)p->d.side * p->d.side * p->d.side;
+  lse_from_global_kernel<<<ceil_div(N, 256), 256, 0, ctx->stream>>>(d_lse, N, p->lse, p->lse2);
+  int rc = after_launch(ctx, "lse_from_global_kernel");
+  if (rc) return rc;
+  finite_sum_kernel<<<1, 256, 0, ctx->stream>>>(p->lse, N, p->red + kRedLL);
+  if ((rc = after_launch(ctx, "finite_sum_kernel"))) return rc;
+  if ((rc = mark_phase(p, 3))) return rc;
+  if ((rc = enqueue_mstep(p, d_model_sum, d_weight_sum))) return rc;
+  const bool det = p->d.insert_mode == EMC_INSERT_DETERMINISTIC;
+  const int nb = (int)std::min<long long>(ceil_div(n3, 256), (long long)ctx->sm_count * 8);
+  sums_out_kernel<<<nb, 256, 0, ctx->stream>>>(det ? p->fix_m : nullptr, p->fix_w,
+                                                p->red + kRedBoundM, p->acc2, d_model_sum,
+                                                d_weight_sum, n3);
+  return after_launch(ctx, "sums_out_kernel");
+}
+
+extern "C" int emc_model_from_sums(emc_plan* p, const float* d_model_sum,
+                                   const float* d_weight_sum, int n_ranks, float* d_model,
+                                   float* d_weight) {
+  if (!p) return EMC_ERR_INVALID;
+  emc_ctx* ctx = p->ctx;
+  EMC_REQUIRE(ctx, d_model_sum && d_weight_sum && d_model && d_weight && n_ranks >= 1,
+              "model_from_sums: bad argument");
+  const long long n3 = (long long)p->d.side * p->d.side * p->d.side;
+  const int nb = (int)std::min<long long>(ceil_div(n3, 256), (long long)ctx->sm_count * 8);
+  model_from_sums_kernel<<<nb, 256, 0, ctx->stream>>>(d_model_sum, d_weight_sum, (float)n_ranks,
+                                                       d_model, d_weight, n3);
+  int rc = after_launch(ctx, "model_from_sums_kernel");
+  if (rc) return rc;
+  if ((rc = mark_phase(p, 5))) return rc;
+  return enqueue_normalise(p, d_model);
 }

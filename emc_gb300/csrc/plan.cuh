@@ -88,6 +88,10 @@ struct emc_plan {
   int* prune_kb_off = nullptr;          // [n_rt + 1] M-step k-blocks per rotation tile
   int* prune_kb_list = nullptr;         // the 64-pattern k-blocks themselves
   void* prune = nullptr;                // PruneState
+  // L holds the normalised responsibilities P of the last iteration (true),
+  // or still its log-likelihoods (false: mprep left P unwritten; it is formed
+  // on request by plan_respons_ready)
+  bool p_written = true;
 
   // one captured iteration (emc_plan_capture / emc_plan_replay)
   cudaGraph_t graph = nullptr;
@@ -105,6 +109,8 @@ struct emc_plan {
   int estep_pair = 1;       // full scans on CTA pairs (EMC_OPT_ESTEP_PAIR)
   int mstep_raster = -16;   // tensor M-step tile order (EMC_OPT_MSTEP_RASTER)
   int mstep_aggregate = 0;  // tensor M-step: warp-aggregated float atomics (nearest)
+  unsigned debug_spin = 0;  // > 0: polls per tensor-pipeline wait (EMC_OPT_DEBUG_SPIN)
+  int mstep_pair = 1;       // tensor M-step full scans on CTA pairs (EMC_OPT_MSTEP_PAIR)
 
   std::vector<void*> allocs;
   size_t bytes = 0;
@@ -179,5 +185,8 @@ int tc_time_estep(emc_plan* p, int raster, int first, int count, float* ms);
 int tc_mstep(emc_plan* p, float* model, float* weight);
 int* tc_status(emc_plan* p);  // device status word of the tensor-core pipelines
 void tc_free(emc_plan* p);
+// Forms P = exp(L - lse) over L on the plan's stream when the last iteration
+// left it unwritten (p_written false); no-op otherwise.
+int plan_respons_ready(emc_plan* p);
 
 }  // namespace emc

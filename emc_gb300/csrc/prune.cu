@@ -340,6 +340,7 @@ static int prune_prepare(emc_plan* p, PruneState* ps, bool reorder) {
   int rc;
   std::vector<int> newpos(N), new_perm = ps->h_perm;
   std::iota(newpos.begin(), newpos.end(), 0);
+  if ((rc = plan_respons_ready(p))) return rc;
   if (reorder) {
     best_rotation_kernel<<<ceil_div(N, 256), 256, 0, ctx->stream>>>(p->L, R, N, ps->d_best);
     if ((rc = after_launch(ctx, "best_rotation_kernel"))) return rc;
@@ -631,6 +632,8 @@ extern "C" int emc_plan_best_quaternions(emc_plan* p, float* d_quats) {
                                   cudaMemcpyHostToDevice, ctx->stream));
     perm = ps->d_perm_res;
   }
+  int rr = plan_respons_ready(p);
+  if (rr) return rr;
   best_quat_kernel<<<ceil_div(N, 256), 256, 0, ctx->stream>>>(p->L, R, N, p->rot, perm, d_quats);
   int rc = after_launch(ctx, "best_quat_kernel");
   if (!rc) EMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));  // the host perm is staged

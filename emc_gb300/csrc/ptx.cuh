@@ -50,11 +50,44 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   return ok != 0;
 }
 
+// try_wait with acquire at cluster scope: for a barrier that threads of the
+// pair peer arrive on (their prior TMEM reads happen before what follows).
+__device__ __forceinline__ bool mbar_try_wait_cluster(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Arrives (release at cluster scope) on the mbarrier at shared::cluster
+// address `bar_cluster`, this CTA's or its pair peer's.
+__device__ __forceinline__ void mbar_arrive_cluster(uint32_t bar_cluster) {
+  asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(bar_cluster)
+               : "memory");
+}
+
 // Bounded wait for the phase with the given parity to complete.  On timeout
-// sets bit `where` of *status and returns false.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* status, int where) {
-  for (uint32_t i = 0; i < kSpinLimit; ++i)
+// sets bit `where` of *status and returns false.  `limit` polls at most (a
+// plan's debug option lowers it for the pipeline waits; the drain waits that
+// make an aborted CTA safe to exit always use kSpinLimit).
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* status, int where,
+                                          uint32_t limit = kSpinLimit) {
+  for (uint32_t i = 0; i < limit; ++i)
     if (mbar_try_wait(bar, parity)) return true;
+  if (status) atomicOr(status, 1 << where);
+  return false;
+}
+
+// mbar_wait at cluster scope (mbar_try_wait_cluster).
+__device__ __forceinline__ bool mbar_wait_cluster(uint64_t* bar, uint32_t parity, int* status,
+                                                  int where, uint32_t limit = kSpinLimit) {
+  for (uint32_t i = 0; i < limit; ++i)
+    if (mbar_try_wait_cluster(bar, parity)) return true;
   if (status) atomicOr(status, 1 << where);
   return false;
 }
@@ -64,13 +97,45 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* s
 // warps take issue slots from the single threads that issue the TMA loads
 // and the MMAs.  Gives up after kSpinLimit polls (seconds).
 __device__ __forceinline__ bool mbar_wait_sleep(uint64_t* bar, uint32_t parity, int* status,
-                                                int where, uint32_t ns) {
-  for (uint32_t i = 0; i < kSpinLimit; ++i) {
+                                                int where, uint32_t ns,
+                                                uint32_t limit = kSpinLimit) {
+  for (uint32_t i = 0; i < limit; ++i) {
     if (mbar_try_wait(bar, parity)) return true;
     __nanosleep(ns);
   }
   if (status) atomicOr(status, 1 << where);
   return false;
+}
+
+// Exit path of a pipeline that gave up (a bounded wait timed out): waits, at
+// the full limit, until the TMA loads of the last `issued` k-blocks have
+// landed, so that no copy into this CTA's shared memory is in flight when the
+// CTA exits.  The loads of k-block it complete phase (it / stages) & 1 of
+// full[it % stages]; each of the last `stages` k-blocks is the newest phase
+// armed on its stage, so a completed phase is recognised by its parity.  When
+// a phase never completes (a CTA pair whose peer stopped issuing leaves bytes
+// outstanding), the wait gives up after kDrainLimit polls
+// and records bit `where`; settle_after_timeout then covers what is left.
+constexpr uint32_t kDrainLimit = 1u << 16;
+__device__ __forceinline__ void drain_loads(uint64_t* full, int stages, uint32_t issued,
+                                            int* status, int where) {
+  const uint32_t first = issued > (uint32_t)stages ? issued - (uint32_t)stages : 0u;
+  for (uint32_t it = first; it < issued; ++it)
+    mbar_wait(&full[it % stages], (it / stages) & 1, status, where, kDrainLimit);
+}
+
+// Last step of every tensor kernel before TMEM is freed.  A CTA pair's loads
+// complete on rank 0's barriers, so rank 1 cannot wait for its own copies,
+// and after a timeout rank 1 may have issued loads for a stage that rank 0
+// never armed; a drain wait may also have given up.  When any bounded wait of
+// the launch gave up (a nonzero status word, read after the CTA's or pair's
+// final barrier), the CTA pauses 200 us -- two orders of magnitude beyond the
+// latency of a TMA copy -- before it frees TMEM and exits.  The normal path
+// reads one word.
+__device__ __forceinline__ void settle_after_timeout(const int* status) {
+  if (!status || *(volatile const int*)status == 0) return;
+  const long long t0 = clock64();
+  while (clock64() - t0 < 400000) __nanosleep(1000);
 }
 
 // ---- TMA ------------------------------------------------------------------

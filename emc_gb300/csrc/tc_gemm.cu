@@ -212,6 +212,7 @@ struct TcEstepArgs {
   float2* part;
   int* bad;
   int* status;
+  uint32_t spin;  // polls per pipeline wait (ptx::kSpinLimit unless a debug option lowers it)
 };
 
 // Epilogue of the likelihood kernels (warps 2 .. 2 + EPI_WARPS - 1): EPI_PARTS
@@ -234,7 +235,7 @@ __device__ __forceinline__ void estep_epilogue(const TcEstepArgs& a, uint32_t tm
   const float ci = nok ? a.cnorm[n] : 1.0f;
   float m = -INFINITY, ssum = 0.0f;
   int nbad = 0;
-  if (ptx::mbar_wait_sleep(accum, 0, a.status, 2, 256)) {
+  if (ptx::mbar_wait_sleep(accum, 0, a.status, 2, 256, a.spin)) {
     ptx::tc_fence_after();
     const uint32_t lane_addr = tmem + ((uint32_t)(quarter * 32) << 16);
     for (int c0 = half * (BN / EPI_PARTS); c0 < (half + 1) * (BN / EPI_PARTS); c0 += 16) {
@@ -305,7 +306,8 @@ __global__ void __launch_bounds__(es::THREADS, 1)
   uint64_t* full = (uint64_t*)(smem + STAGES * STAGE_BYTES);
   uint64_t* empty = full + STAGES;
   uint64_t* accum = empty + STAGES;
-  uint32_t* tmem_slot = (uint32_t*)(accum + 1);
+  uint64_t* drain = accum + 1;  // the MMA issuer's own completion wait before TMEM is freed
+  uint32_t* tmem_slot = (uint32_t*)(drain + 1);
   float* s_A = (float*)(smem + STAGES * STAGE_BYTES + 256);
   float* s_scale = s_A + BN;
   float* s_lw = s_scale + BN;
@@ -330,6 +332,7 @@ __global__ void __launch_bounds__(es::THREADS, 1)
       ptx::mbar_init(&empty[s], 1);
     }
     ptx::mbar_init(accum, 1);
+    ptx::mbar_init(drain, 1);
     ptx::fence_mbar_init();
   }
   if (threadIdx.x < BN) {
@@ -354,10 +357,11 @@ __global__ void __launch_bounds__(es::THREADS, 1)
     // ------------------------------------------------ TMA producer
     if (lane == 0) {
       const CUtensorMap* maps[kSlots] = {&mK, &mK2h, &mK2l, &mGh, &mMS, &mHh, &mMp, &mGl, &mHl};
-      for (int kb = 0; kb < a.nkb; ++kb) {
+      int kb = 0;
+      for (; kb < a.nkb; ++kb) {
         const int s = kb % STAGES;
         const uint32_t ph = (kb / STAGES) & 1;
-        if (!ptx::mbar_wait(&empty[s], ph ^ 1, a.status, 0)) break;
+        if (!ptx::mbar_wait(&empty[s], ph ^ 1, a.status, 0, a.spin)) break;
         const bool lo = flags[kb] != 0;
         const int ntiles = kSlots - (lo ? 0 : 1) - (glo ? 0 : 1) - (hlo ? 0 : 1);
         ptx::mbar_arrive_expect_tx(&full[s], ntiles * TILE_BYTES);
@@ -368,6 +372,9 @@ __global__ void __launch_bounds__(es::THREADS, 1)
           ptx::tma_load_2d(st + j * TILE_BYTES, maps[j], kb * BK, j < sGh ? n0 : r0, &full[s]);
         }
       }
+      // no copy may still be landing in shared memory when the CTA exits
+      // (after a normal run the MMAs have consumed them all: no wait)
+      ptx::drain_loads(full, STAGES, (uint32_t)kb, a.status, 11);
     }
   } else if (warp == 1) {
     // ------------------------------------------------ MMA issuer
@@ -377,7 +384,7 @@ __global__ void __launch_bounds__(es::THREADS, 1)
       for (int kb = 0; kb < a.nkb; ++kb) {
         const int s = kb % STAGES;
         const uint32_t ph = (kb / STAGES) & 1;
-        if (!ptx::mbar_wait(&full[s], ph, a.status, 1)) break;
+        if (!ptx::mbar_wait(&full[s], ph, a.status, 1, a.spin)) break;
         ptx::tc_fence_after();
         const bool lo = flags[kb] != 0;
         const uint32_t base = ptx::smem_u32(smem + s * STAGE_BYTES);
@@ -398,12 +405,18 @@ __global__ void __launch_bounds__(es::THREADS, 1)
       // fires when every MMA issued above has completed; after a timeout the
       // epilogue's own bounded wait reports it
       ptx::mma_commit(accum);
+      // TMEM is freed only after every MMA issued here has completed, also
+      // when the epilogue stopped waiting
+      ptx::mma_commit(drain);
+      ptx::mbar_wait(drain, 0, a.status, 12);
     }
   } else {
     // ------------------------------------------------ epilogue (warps 2-17)
     estep_epilogue(a, tmem, accum, s_A, s_scale, s_lw, s_half, warp, lane, n0, r0, rt);
   }
   ptx::tc_fence_before();
+  __syncthreads();
+  if (threadIdx.x == 32) ptx::settle_after_timeout(a.status);
   __syncthreads();
   if (warp == 1) {
     ptx::tc_fence_after();
@@ -452,7 +465,8 @@ __global__ void __launch_bounds__(es::THREADS, 1)
   uint64_t* full = (uint64_t*)(smem + STAGES * STAGE_BYTES);
   uint64_t* empty = full + STAGES;
   uint64_t* accum = empty + STAGES;
-  uint32_t* tmem_slot = (uint32_t*)(accum + 1);
+  uint64_t* drain = accum + 1;  // rank 0's MMA issuer waits on it before TMEM is freed
+  uint32_t* tmem_slot = (uint32_t*)(drain + 1);
   float* s_A = (float*)(smem + STAGES * STAGE_BYTES + 256);
   float* s_scale = s_A + BN;
   float* s_lw = s_scale + BN;
@@ -474,6 +488,7 @@ __global__ void __launch_bounds__(es::THREADS, 1)
       ptx::mbar_init(&empty[s], 1);
     }
     ptx::mbar_init(accum, 1);
+    ptx::mbar_init(drain, 1);
     ptx::fence_mbar_init();
   }
   if (threadIdx.x < BN) {
@@ -503,10 +518,11 @@ __global__ void __launch_bounds__(es::THREADS, 1)
     if (lane == 0) {
       const CUtensorMap* mb1 = rank ? &mMS : &mGh;
       const CUtensorMap* mb2 = rank ? &mMp : &mHh;
-      for (int kb = 0; kb < a.nkb; ++kb) {
+      int kb = 0;
+      for (; kb < a.nkb; ++kb) {
         const int s = kb % STAGES;
         const uint32_t ph = (kb / STAGES) & 1;
-        if (!ptx::mbar_wait(&empty[s], ph ^ 1, a.status, 0)) break;
+        if (!ptx::mbar_wait(&empty[s], ph ^ 1, a.status, 0, a.spin)) break;
         const bool lo = flags0[kb] != 0 || (flags1 && flags1[kb] != 0);
         const uint32_t bytes = (lo ? 5 : 4) * es2::TILE + (glo ? es2::HALF : 0);
         if (rank == 0) ptx::mbar_arrive_expect_tx(&full[s], 2 * bytes);  // both CTAs' loads
@@ -520,6 +536,8 @@ __global__ void __launch_bounds__(es::THREADS, 1)
         ptx::tma_load_2d_pair(st + es2::oB2, mb2, x, r0, fb);
         if (glo) ptx::tma_load_2d_pair(st + es2::oGl, &mGl64, x, r0 + 64 * (int)rank, fb);
       }
+      // rank 0's barriers count both CTAs' bytes of the stages it armed
+      if (rank == 0) ptx::drain_loads(full, STAGES, (uint32_t)kb, a.status, 11);
     }
   } else if (warp == 1) {
     // ------------------------------------------------ MMA issuer (rank 0)
@@ -529,7 +547,7 @@ __global__ void __launch_bounds__(es::THREADS, 1)
       for (int kb = 0; kb < a.nkb; ++kb) {
         const int s = kb % STAGES;
         const uint32_t ph = (kb / STAGES) & 1;
-        if (!ptx::mbar_wait(&full[s], ph, a.status, 1)) break;
+        if (!ptx::mbar_wait(&full[s], ph, a.status, 1, a.spin)) break;
         ptx::tc_fence_after();
         const bool lo = flags0[kb] != 0 || (flags1 && flags1[kb] != 0);
         const uint32_t base = ptx::smem_u32(smem + s * STAGE_BYTES);
@@ -545,6 +563,8 @@ __global__ void __launch_bounds__(es::THREADS, 1)
         ptx::mma_commit_pair(&empty[s], 0x3);
       }
       ptx::mma_commit_pair(accum, 0x3);
+      ptx::mma_commit_pair(drain, 0x1);  // both CTAs' TMEM is written by these MMAs
+      ptx::mbar_wait(drain, 0, a.status, 12);
     }
   } else {
     // ------------------------------------------------ epilogue (warps 2-17)
@@ -553,6 +573,8 @@ __global__ void __launch_bounds__(es::THREADS, 1)
   ptx::tc_fence_before();
   __syncthreads();
   ptx::cluster_sync();  // the pair's MMAs and barrier traffic are over in both CTAs
+  if (threadIdx.x == 32) ptx::settle_after_timeout(a.status);
+  __syncthreads();
   if (warp == 1) {
     ptx::tc_fence_after();
     ptx::tmem_dealloc_pair(tmem, 512);
@@ -594,6 +616,7 @@ struct TcEstepPoisArgs {
   float* PHI;
   float2* part;
   int* status;
+  uint32_t spin;  // polls per pipeline wait
 };
 
 __global__ void __launch_bounds__(ep::THREADS, 1)
@@ -606,7 +629,8 @@ __global__ void __launch_bounds__(ep::THREADS, 1)
   uint64_t* full = (uint64_t*)(smem + STAGES * STAGE_BYTES);
   uint64_t* empty = full + STAGES;
   uint64_t* accum = empty + STAGES;
-  uint32_t* tmem_slot = (uint32_t*)(accum + 1);
+  uint64_t* drain = accum + 1;  // the MMA issuer's own completion wait before TMEM is freed
+  uint32_t* tmem_slot = (uint32_t*)(drain + 1);
   float* s_ss = (float*)(smem + STAGES * STAGE_BYTES + 256);
   float* s_lw = s_ss + BN;
 
@@ -627,6 +651,7 @@ __global__ void __launch_bounds__(ep::THREADS, 1)
       ptx::mbar_init(&empty[s], 1);
     }
     ptx::mbar_init(accum, 1);
+    ptx::mbar_init(drain, 1);
     ptx::fence_mbar_init();
   }
   for (int c = threadIdx.x; c < BN; c += blockDim.x) {
@@ -646,16 +671,18 @@ __global__ void __launch_bounds__(ep::THREADS, 1)
   if (warp == 0) {
     // ------------------------------------------------ TMA producer
     if (lane == 0) {
-      for (int kb = 0; kb < a.nkb; ++kb) {
+      int kb = 0;
+      for (; kb < a.nkb; ++kb) {
         const int s = kb % STAGES;
         const uint32_t ph = (kb / STAGES) & 1;
-        if (!ptx::mbar_wait(&empty[s], ph ^ 1, a.status, 8)) break;
+        if (!ptx::mbar_wait(&empty[s], ph ^ 1, a.status, 8, a.spin)) break;
         ptx::mbar_arrive_expect_tx(&full[s], STAGE_BYTES);
         unsigned char* st = smem + s * STAGE_BYTES;
         ptx::tma_load_2d(st, &mK, kb * BK, n0, &full[s]);
         ptx::tma_load_2d(st + A_BYTES, &mLh, kb * BK, r0, &full[s]);
         ptx::tma_load_2d(st + A_BYTES + B_BYTES, &mLl, kb * BK, r0, &full[s]);
       }
+      ptx::drain_loads(full, STAGES, (uint32_t)kb, a.status, 11);  // none in flight at exit
     }
   } else if (warp == 1) {
     // ------------------------------------------------ MMA issuer
@@ -664,7 +691,7 @@ __global__ void __launch_bounds__(ep::THREADS, 1)
       for (int kb = 0; kb < a.nkb; ++kb) {
         const int s = kb % STAGES;
         const uint32_t ph = (kb / STAGES) & 1;
-        if (!ptx::mbar_wait(&full[s], ph, a.status, 9)) break;
+        if (!ptx::mbar_wait(&full[s], ph, a.status, 9, a.spin)) break;
         ptx::tc_fence_after();
         const uint32_t base = ptx::smem_u32(smem + s * STAGE_BYTES);
 #pragma unroll
@@ -678,6 +705,8 @@ __global__ void __launch_bounds__(ep::THREADS, 1)
         ptx::mma_commit(&empty[s]);
       }
       ptx::mma_commit(accum);
+      ptx::mma_commit(drain);  // TMEM is freed only after these MMAs have completed
+      ptx::mbar_wait(drain, 0, a.status, 12);
     }
   } else {
     // ------------------------------------------------ epilogue (warps 2-9)
@@ -687,7 +716,7 @@ __global__ void __launch_bounds__(ep::THREADS, 1)
     const bool nok = n < a.N;
     const float ci = nok ? a.cnorm[n] : 1.0f;
     const float Ki = nok ? a.Ksum[n] : 0.0f;
-    const bool waited = ptx::mbar_wait_sleep(accum, 0, a.status, 10, 256);
+    const bool waited = ptx::mbar_wait_sleep(accum, 0, a.status, 10, 256, a.spin);
     if (waited) ptx::tc_fence_after();
     const uint32_t lane_addr = tmem + ((uint32_t)(quarter * 32) << 16);
     {
@@ -733,6 +762,8 @@ __global__ void __launch_bounds__(ep::THREADS, 1)
   }
   ptx::tc_fence_before();
   __syncthreads();
+  if (threadIdx.x == 32) ptx::settle_after_timeout(a.status);
+  __syncthreads();
   if (warp == 1) {
     ptx::tc_fence_after();
     ptx::tmem_dealloc(tmem, BN);
@@ -774,6 +805,7 @@ struct TcMstepArgs {
   const int* kb_off;
   const int* kb_list;
   int* status;
+  uint32_t spin;  // polls per pipeline wait
 };
 
 // The k-blocks of rotation tile rt: count, and the j-th of them.
@@ -878,7 +910,8 @@ __global__ void __launch_bounds__(ms::THREADS, 1)
   uint64_t* empty = full + STAGES;
   uint64_t* tfull = empty + STAGES;  // [2] accumulator ready
   uint64_t* tempty = tfull + 2;      // [2] accumulator drained (one arrival per epilogue warp)
-  uint32_t* tmem_slot = (uint32_t*)(tempty + 2);
+  uint64_t* drain = tempty + 2;      // the MMA issuer's own completion wait before TMEM is freed
+  uint32_t* tmem_slot = (uint32_t*)(drain + 1);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (threadIdx.x == 0) {
@@ -890,6 +923,7 @@ __global__ void __launch_bounds__(ms::THREADS, 1)
       ptx::mbar_init(&tfull[b], 1);
       ptx::mbar_init(&tempty[b], EPI_WARPS);
     }
+    ptx::mbar_init(drain, 1);
     ptx::fence_mbar_init();
   }
   if (warp == 1) {
@@ -914,7 +948,7 @@ __global__ void __launch_bounds__(ms::THREADS, 1)
           const int kb = ms_kb(a, r0 / BM, j);
           const int s = it % STAGES;
           const uint32_t ph = (it / STAGES) & 1;
-          if (!ptx::mbar_wait(&empty[s], ph ^ 1, a.status, 4)) {
+          if (!ptx::mbar_wait(&empty[s], ph ^ 1, a.status, 4, a.spin)) {
             ok = false;
             break;
           }
@@ -925,6 +959,7 @@ __global__ void __launch_bounds__(ms::THREADS, 1)
           ptx::tma_load_2d(st + 2 * A_BYTES, &mKt, kb * BK, q0, &full[s]);
         }
       }
+      ptx::drain_loads(full, STAGES, it, a.status, 11);  // none in flight at exit
     }
   } else if (warp == 1) {
     // ------------------------------------------------ MMA issuer
@@ -936,7 +971,7 @@ __global__ void __launch_bounds__(ms::THREADS, 1)
       for (int t = blockIdx.x; t < a.n_tiles && ok; t += gridDim.x, ++j) {
         const int b = j & 1;
         const uint32_t d = tmem + (uint32_t)(b * BN);
-        if (!ptx::mbar_wait(&tempty[b], ((j >> 1) & 1) ^ 1, a.status, 7)) break;
+        if (!ptx::mbar_wait(&tempty[b], ((j >> 1) & 1) ^ 1, a.status, 7, a.spin)) break;
         ptx::tc_fence_after();
         int r0t, q0t;
         ms_tile(a, t, r0t, q0t);
@@ -946,7 +981,7 @@ __global__ void __launch_bounds__(ms::THREADS, 1)
         for (int kb = 0; kb < nk; ++kb, ++it) {
           const int s = it % STAGES;
           const uint32_t ph = (it / STAGES) & 1;
-          if (!ptx::mbar_wait(&full[s], ph, a.status, 5)) {
+          if (!ptx::mbar_wait(&full[s], ph, a.status, 5, a.spin)) {
             ok = false;
             break;
           }
@@ -964,6 +999,8 @@ __global__ void __launch_bounds__(ms::THREADS, 1)
         }
         ptx::mma_commit(&tfull[b]);  // fires when this tile's MMAs have completed
       }
+      ptx::mma_commit(drain);  // TMEM is freed only after every MMA issued here has completed
+      ptx::mbar_wait(drain, 0, a.status, 12);
     }
   } else {
     // ------------------------------------------------ insertion epilogue (warps 2-9)
@@ -982,7 +1019,7 @@ __global__ void __launch_bounds__(ms::THREADS, 1)
       const bool live = rok && Tr > 1e-10f;
       RotMat Rm = {};
       if (rok) Rm = quat_to_matrix(a.rot + 4 * (size_t)r);
-      if (!ptx::mbar_wait_sleep(&tfull[b], (j >> 1) & 1, a.status, 6, 128)) break;
+      if (!ptx::mbar_wait_sleep(&tfull[b], (j >> 1) & 1, a.status, 6, 128, a.spin)) break;
       ptx::tc_fence_after();
       const uint32_t lane_addr = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(b * BN);
       for (int c0 = half * 128; c0 < half * 128 + 128; c0 += 16) {
@@ -1009,15 +1046,206 @@ __global__ void __launch_bounds__(ms::THREADS, 1)
   }
   ptx::tc_fence_before();
   __syncthreads();
+  if (threadIdx.x == 32) ptx::settle_after_timeout(a.status);
+  __syncthreads();
   if (warp == 1) {
     ptx::tc_fence_after();
     ptx::tmem_dealloc(tmem, 512);
   }
 }
 
+// ------------------------------------------------- M-step on CTA pairs -----
+// The M-step's tiles as 256 rotations x 256 pixels per cluster of two CTAs:
+// 256-row MMAs (cta_group::2) issued by rank 0, each CTA holding the Q rows
+// of its own 128 rotations and 128 of the tile's 256 pixel rows of K^T.  Per
+// 64-pattern stage a CTA loads 32 KB instead of 48 KB for the same MMA work
+// and its tensor core reads half of the pixel-side operand.  Persistent over
+// the cluster's tiles; each CTA's TMEM holds its 128 rotations x 256 pixels,
+// double-buffered (2 x 256 columns), so the insertion epilogue of one tile
+// overlaps the MMAs of the next.  Both CTAs' loads complete on rank 0's
+// `full` barriers; rank 0's commits multicast to both CTAs' `empty` and
+// `tfull`; the epilogue warps of both CTAs hand a buffer back on rank 0's
+// `tempty`.  Full scans only (a pruned M-step runs single CTAs).
+namespace ms2 {
+constexpr int STAGES = 4;
+constexpr int A_BYTES = ms::BM * ms::BK * 2;        // 16 KB: 128 rotations x 64 patterns
+constexpr int B_BYTES = 128 * ms::BK * 2;           // 16 KB: 128 pixels x 64 patterns
+constexpr int STAGE_BYTES = 2 * A_BYTES + B_BYTES;  // Q hi, Q lo, K^T half
+constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 256 + 1024;
+static_assert(SMEM_BYTES <= 232448, "shared memory of the pair M-step");
+}  // namespace ms2
+
+__global__ void __launch_bounds__(ms::THREADS, 1)
+    tc_mstep_pair_kernel(const __grid_constant__ CUtensorMap mQh,
+                         const __grid_constant__ CUtensorMap mQl,
+                         const __grid_constant__ CUtensorMap mKt128, TcMstepArgs a) {
+  using namespace ms;
+  using ms2::STAGES;
+  using ms2::STAGE_BYTES;
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint64_t* full = (uint64_t*)(smem + STAGES * STAGE_BYTES);
+  uint64_t* empty = full + STAGES;
+  uint64_t* tfull = empty + STAGES;  // [2] accumulator ready (both CTAs)
+  uint64_t* tempty = tfull + 2;      // [2] rank 0: accumulator drained by both CTAs
+  uint64_t* drain = tempty + 2;      // rank 0's MMA issuer waits on it before TMEM is freed
+  uint32_t* tmem_slot = (uint32_t*)(drain + 1);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t rank = ptx::cluster_ctarank();
+  const int cl = (int)(blockIdx.x >> 1), ncl = (int)(gridDim.x >> 1);
+  const int n_rp = (a.n_rt + 1) / 2;  // rotation-tile pairs
+  const int n_tiles = n_rp * a.n_qt;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      ptx::mbar_init(&full[s], 1);
+      ptx::mbar_init(&empty[s], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      ptx::mbar_init(&tfull[b], 1);
+      ptx::mbar_init(&tempty[b], 2 * EPI_WARPS);
+    }
+    ptx::mbar_init(drain, 1);
+    ptx::fence_mbar_init();
+  }
+  if (warp == 1) {
+    ptx::tmem_alloc_pair(tmem_slot, 512);
+    ptx::tmem_relinquish_pair();
+  }
+  ptx::tc_fence_before();
+  __syncthreads();
+  ptx::cluster_sync();  // both CTAs' barriers initialised and TMEM allocated
+  ptx::tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0) {
+    // ------------------------------------------------ TMA producer (both CTAs)
+    if (lane == 0) {
+      uint32_t it = 0;
+      bool ok = true;
+      const uint32_t bytes = (a.q_lo ? 2 : 1) * ms2::A_BYTES + ms2::B_BYTES;
+      for (int t = cl; t < n_tiles && ok; t += ncl) {
+        int qt, rp;
+        raster_tile(t, a.raster, a.n_qt, n_rp, qt, rp);
+        const int r0 = (2 * rp + (int)rank) * BM, q0 = qt * BN + 128 * (int)rank;
+        for (int kb = 0; kb < a.nkb; ++kb, ++it) {
+          const int s = it % STAGES;
+          const uint32_t ph = (it / STAGES) & 1;
+          if (!ptx::mbar_wait(&empty[s], ph ^ 1, a.status, 4, a.spin)) {
+            ok = false;
+            break;
+          }
+          if (rank == 0) ptx::mbar_arrive_expect_tx(&full[s], 2 * bytes);  // both CTAs' loads
+          const uint32_t fb = ptx::mapa_shared(ptx::smem_u32(&full[s]), 0);
+          unsigned char* st = smem + s * STAGE_BYTES;
+          ptx::tma_load_2d_pair(st, &mQh, kb * BK, r0, fb);
+          if (a.q_lo) ptx::tma_load_2d_pair(st + ms2::A_BYTES, &mQl, kb * BK, r0, fb);
+          ptx::tma_load_2d_pair(st + 2 * ms2::A_BYTES, &mKt128, kb * BK, q0, fb);
+        }
+      }
+      // rank 0's barriers count both CTAs' bytes of the stages it armed
+      if (rank == 0) ptx::drain_loads(full, STAGES, it, a.status, 11);
+    }
+  } else if (warp == 1) {
+    // ------------------------------------------------ MMA issuer (rank 0)
+    if (rank == 0 && lane == 0) {
+      constexpr uint32_t idesc = ptx::idesc_f16(2 * BM, BN);  // 256 x 256
+      uint32_t it = 0;
+      bool ok = true;
+      int j = 0;
+      for (int t = cl; t < n_tiles && ok; t += ncl, ++j) {
+        const int b = j & 1;
+        const uint32_t d = tmem + (uint32_t)(b * BN);
+        if (!ptx::mbar_wait_cluster(&tempty[b], ((j >> 1) & 1) ^ 1, a.status, 7, a.spin)) break;
+        ptx::tc_fence_after();
+        for (int kb = 0; kb < a.nkb; ++kb, ++it) {
+          const int s = it % STAGES;
+          const uint32_t ph = (it / STAGES) & 1;
+          if (!ptx::mbar_wait(&full[s], ph, a.status, 5, a.spin)) {
+            ok = false;
+            break;
+          }
+          ptx::tc_fence_after();
+          const uint32_t base = ptx::smem_u32(smem + s * STAGE_BYTES);
+#pragma unroll
+          for (int ks = 0; ks < BK / 16; ++ks) {
+            const uint64_t dQh = ptx::smem_desc(base + ks * 32, 1024, 2);
+            const uint64_t dQl = ptx::smem_desc(base + ms2::A_BYTES + ks * 32, 1024, 2);
+            const uint64_t dK = ptx::smem_desc(base + 2 * ms2::A_BYTES + ks * 32, 1024, 2);
+            ptx::mma_f16_pair(d, dQh, dK, idesc, (kb | ks) ? 1u : 0u);
+            if (a.q_lo) ptx::mma_f16_pair(d, dQl, dK, idesc, 1u);
+          }
+          ptx::mma_commit_pair(&empty[s], 0x3);
+        }
+        ptx::mma_commit_pair(&tfull[b], 0x3);  // fires when this tile's MMAs have completed
+      }
+      ptx::mma_commit_pair(drain, 0x1);  // both CTAs' TMEM is written by these MMAs
+      ptx::mbar_wait(drain, 0, a.status, 12);
+    }
+  } else {
+    // ------------------------------------------------ insertion epilogue (warps 2-9)
+    const int quarter = warp & 3;      // TMEM lanes this warp may access
+    const int half = (warp - 2) >> 2;  // which 128 of the tile's 256 columns
+    const int rl = quarter * 32 + lane;
+    const uint32_t back = rank == 0 ? 0u : 1u;
+    int j = 0;
+    for (int t = cl; t < n_tiles; t += ncl, ++j) {
+      const int b = j & 1;
+      int qt, rp;
+      raster_tile(t, a.raster, a.n_qt, n_rp, qt, rp);
+      const int r0 = (2 * rp + (int)rank) * BM, q0 = qt * BN;  // TMEM column c: pixel q0 + c
+      const int r = r0 + rl;
+      const bool rok = r < a.R;
+      const float Tr = rok ? a.T[r] : 0.0f;
+      const float qs = rok ? a.qscale[r] : 0.0f;
+      const bool live = rok && Tr > 1e-10f;
+      RotMat Rm = {};
+      if (rok) Rm = quat_to_matrix(a.rot + 4 * (size_t)r);
+      if (!ptx::mbar_wait_sleep(&tfull[b], (j >> 1) & 1, a.status, 6, 128, a.spin)) break;
+      ptx::tc_fence_after();
+      const uint32_t lane_addr = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(b * BN);
+      for (int c0 = half * 128; c0 < half * 128 + 128; c0 += 16) {
+        float u[16];
+        ptx::tmem_ld16(lane_addr + c0, u);
+        ptx::tmem_wait_ld();
+        if (q0 + c0 >= a.P_eff) continue;  // padding columns (uniform over the warp)
+#pragma unroll
+        for (int jj = 0; jj < 16; ++jj) {
+          const int q = q0 + c0 + jj;
+          if (q < a.P_eff) {
+            const float U = u[jj] * qs;
+            const float slice = live ? U / Tr : 0.0f;
+            tc_insert(a, Rm, live, __ldg(a.cx + q), __ldg(a.cy + q), __ldg(a.cz + q), Tr * slice,
+                      Tr);
+          }
+        }
+      }
+      // this warp's reads of buffer b are complete: hand it back to rank 0's MMA warp
+      ptx::tc_fence_before();
+      __syncwarp();
+      if (lane == 0) {
+        if (back)
+          ptx::mbar_arrive_cluster(ptx::mapa_shared(ptx::smem_u32(&tempty[b]), 0));
+        else
+          ptx::mbar_arrive(&tempty[b]);
+      }
+    }
+  }
+  ptx::tc_fence_before();
+  __syncthreads();
+  ptx::cluster_sync();  // the pair's MMAs and barrier traffic are over in both CTAs
+  if (threadIdx.x == 32) ptx::settle_after_timeout(a.status);
+  __syncthreads();
+  if (warp == 1) {
+    ptx::tc_fence_after();
+    ptx::tmem_dealloc_pair(tmem, 512);
+  }
+}
+
 // ------------------------------------------------------------ host -------
 struct TcState {
   CUtensorMap mK, mK2h, mK2l, mQh, mQl, mKt;
+  CUtensorMap mKt128;  // K^T in 128-row boxes (pair M-step halves)
   CUtensorMap rot[6];    // M', MS, Gh, Gl, Hh, Hl: 128-row boxes
   CUtensorMap gl64;        // G lo: 64-row boxes (CTA-pair halves)
   CUtensorMap mLh, mLl;  // true Poisson: log-slices hi / lo (in Gh, Gl), 256-row boxes
@@ -1084,6 +1312,7 @@ int tc_bind(emc_plan* p) {
     }
     if (!rc) rc = make_map(ctx, &st->mQh, p->Qh, Rp, Np, 128, 64);
     if (!rc) rc = make_map(ctx, &st->mKt, p->KhT, Kp, Np, 256, 64);
+    if (!rc) rc = make_map(ctx, &st->mKt128, p->KhT, Kp, Np, 128, 64);
     if (rc) return rc;
     EMC_CUDA(ctx, cudaFuncSetAttribute(tc_estep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        es::SMEM_BYTES));
@@ -1094,6 +1323,9 @@ int tc_bind(emc_plan* p) {
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, ep::SMEM_BYTES));
     EMC_CUDA(ctx, cudaFuncSetAttribute(tc_mstep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        ms::SMEM_BYTES));
+    EMC_CUDA(ctx, cudaFuncSetAttribute(tc_mstep_pair_kernel,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       ms2::SMEM_BYTES));
   }
   if (p->mstep_q_lo && (rc = tc_ensure_qlo(p))) return rc;
   // counts already in FP16 from the bind's pattern pass when its scale holds
@@ -1161,6 +1393,7 @@ static int estep_pois_launch(emc_plan* p, int raster, int first, int count, bool
   a.PHI = p->PHI;
   a.part = p->part;
   a.status = st->status;
+  a.spin = p->debug_spin ? p->debug_spin : ptx::kSpinLimit;
   const int total = a.n_pt * a.n_rt;
   first = a.tiles ? 0 : std::max(0, std::min(first, total));
   const int grid = a.tiles ? p->prune_n_tiles : std::min(total - first, count);
@@ -1200,6 +1433,7 @@ static int estep_launch(emc_plan* p, int raster, int first, int count, bool full
   a.part = p->part;
   a.bad = p->flags + 4;
   a.status = st->status;
+  a.spin = p->debug_spin ? p->debug_spin : ptx::kSpinLimit;
   const CUtensorMap* rm = st->rot;
   if (p->estep_pair && !a.tiles && !(a.gh_lo & 2)) {
     // CTA pairs: tiles are (pattern-tile pair, rotation tile)
@@ -1393,7 +1627,31 @@ int tc_mstep(emc_plan* p, float* model, float* weight) {
   a.kb_list = p->prune_kb_list;
   a.bounds = p->red + kRedBoundM;
   a.status = st->status;
+  a.spin = p->debug_spin ? p->debug_spin : ptx::kSpinLimit;
   a.n_tiles = a.n_qt * a.n_rt;
+  if (p->mstep_pair && !a.kb_off && a.n_rt > 1 && ctx->sm_count >= 2) {
+    // CTA pairs, persistent: one cluster per two SMs
+    const int tiles = ((a.n_rt + 1) / 2) * a.n_qt;
+    const int clusters = std::min(tiles, ctx->sm_count / 2);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(2 * clusters);
+    cfg.blockDim = dim3(ms::THREADS);
+    cfg.dynamicSmemBytes = ms2::SMEM_BYTES;
+    cfg.stream = ctx->stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = 2;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    const cudaError_t e =
+        cudaLaunchKernelEx(&cfg, tc_mstep_pair_kernel, st->mQh, st->mQl, st->mKt128, a);
+    if (e == cudaSuccess) return after_launch(ctx, "tc_mstep_pair_kernel");
+    // a refused launch configuration is not a sticky error: single CTAs from now on
+    (void)cudaGetLastError();
+    p->mstep_pair = 0;
+  }
   const int grid = std::min(a.n_tiles, ctx->sm_count);
   tc_mstep_kernel<<<grid, ms::THREADS, ms::SMEM_BYTES, ctx->stream>>>(st->mQh, st->mQl, st->mKt, a);
   return after_launch(ctx, "tc_mstep_kernel");

@@ -469,6 +469,23 @@ int emc_batch_destroy(emc_batch* batch);
  * on it (with deterministic insertion, bit for bit).  At 128^3 and 256^3 the
  * default is 5-6 % faster than groups of 8 rotation tiles. */
 #define EMC_OPT_MSTEP_RASTER 8
+/* EMC_OPT_DEBUG_SPIN: test aid, no counterpart in the reference.  value > 0
+ * caps every wait of the tensor-core pipelines (TMA ring, MMA completion,
+ * accumulator hand-over) at `value` polls instead of the default 2^24, so
+ * that a test can make them run out; 0 restores the default.  A wait that
+ * runs out sets the plan's status and emc_plan_wait / emc_iterate return
+ * EMC_ERR_TIMEOUT.  The waits on the way out are not capped: a CTA whose
+ * pipeline gave up first waits until every TMA load it armed has landed and
+ * every MMA it issued has completed, and a CTA pair pauses 200 us before it
+ * frees its TMEM and exits, so no copy or MMA is in flight when a CTA leaves.
+ * The next iteration with the default is unaffected. */
+#define EMC_OPT_DEBUG_SPIN 9
+/* EMC_OPT_MSTEP_PAIR: 1 (default) runs the full-scan tensor-core M-step on
+ * clusters of two CTAs (256 rotations x 256 pixels per pair, 256-row MMAs),
+ * 0 on single CTAs (128 x 256).  Pruned iterations always use single CTAs;
+ * where a cluster launch is refused the plan falls back to single CTAs.
+ * Results do not depend on it (bit for bit with deterministic insertion). */
+#define EMC_OPT_MSTEP_PAIR 10
 int emc_plan_set_option(emc_plan* plan, int option, int value);
 /* Tile-order autotuner of the tensor-core likelihood kernel: expands d_model
  * (sigma as in emc_iterate), times the kernel for each candidate
@@ -503,9 +520,48 @@ int emc_plan_phase_ms(emc_plan* plan, float* ms, int n);
 int emc_tc_gemm_selftest(emc_ctx* ctx, const void* d_a, const void* d_b, float* d_d, int n, int k);
 /* Device pointers into the plan's workspace (valid until the next call):
  * the normalised responsibilities [R*N] (rotation-major) and scaling [R*N]
- * of the last iteration, and the per-pattern lse [N] (double). */
+ * of the last iteration, and the per-pattern lse [N] (double).  An iteration
+ * writes the responsibilities only where the plan itself reads them back
+ * (pruning); otherwise the first request for them (d_respons non-NULL) forms
+ * them from the log-likelihoods with a kernel queued on the plan's stream,
+ * so read them after that stream (emc_sync). */
 int emc_plan_results(emc_plan* plan, const float** d_respons, const float** d_scaling,
                      const double** d_lse);
+
+/* ---- one rank of a rotation split ---------------------------------------
+ * The reference divides the rotations among MPI ranks (main.cpp:141-154):
+ * each rank evaluates its range, the per-pattern maximum and sum of exp are
+ * exchanged (main.cpp:367-392: MPI_MAX, then MPI_SUM of the rescaled sums),
+ * each rank runs the M-step of its range with the global normaliser, and the
+ * model and weight sums are all-reduced and divided by the number of ranks
+ * before model / weight and normalisation (main.cpp:463-476).  A rank's plan
+ * is an ordinary plan over its own rotations (rot / rot_weights at the start
+ * of its range, n_rot = its count).  The three calls are asynchronous on the
+ * plan's stream (emc_plan_wait reports pipeline timeouts); pruning is not
+ * supported here.
+ *
+ * emc_rank_estep: expand, scaling and likelihood over the plan's rotations;
+ *   d_max[N] = max_r L_ri (float) and d_sumexp[N] = sum_r exp(L_ri - max)
+ *   (FP64) over them.  The caller forms lse_i = M + log sum_k s_k exp(m_k - M)
+ *   over the ranks k, M = max_k m_k (FP64).  Replaces the rank's
+ *   cuda_get_slices / cuda_update_scaling_full / cuda_calculate_responsabilities
+ *   / cuda_max_vector / cuda_respons_max_expf sequence (main.cpp:284-380). */
+int emc_rank_estep(emc_plan* plan, float* d_model, float sigma, float* d_max,
+                   double* d_sumexp);
+/* emc_rank_mstep: with the global lse[N] (FP64), the rank's responsibilities
+ * and its M-step + insertion; writes the rank's un-normalised sums
+ * d_model_sum[s^3] (sum of T_r x slice) and d_weight_sum[s^3] (sum of T_r)
+ * for the all-reduce.  Replaces cuda_norm_respons_sumexpf and the
+ * cuda_update_slices loop (main.cpp:384-462). */
+int emc_rank_mstep(emc_plan* plan, const double* d_lse, float* d_model_sum,
+                   float* d_weight_sum);
+/* emc_model_from_sums: from the sums all-reduced over n_ranks ranks: weight =
+ * weight_sum / n_ranks, model = (model_sum / n_ranks) / weight (-1 where the
+ * weight is 0), then the model normalised to a positive mean of 1 and
+ * blurred as the plan's desc asks (main.cpp:467-476).  With n_ranks = 1 and
+ * one rank holding all rotations the three calls give emc_iterate's model. */
+int emc_model_from_sums(emc_plan* plan, const float* d_model_sum, const float* d_weight_sum,
+                        int n_ranks, float* d_model, float* d_weight);
 
 #ifdef __cplusplus
 }

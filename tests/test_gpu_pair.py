@@ -80,3 +80,36 @@ def test_pair_autotune_and_window(ctx, cuda):
     raster, t = plan.autotune(m, 0.3)
     assert raster != 0 and t > 0
     plan.close()
+
+
+def run_mstep(ctx, prob, dev, pair, q_lo=0, raster=-16):
+    s, R, N = prob.cfg.side, prob.quats.shape[0], prob.images.shape[0]
+    plan = E.Plan(ctx, s, N, R, precision=E.PREC_MIXED, insert_mode=E.INSERT_DETERMINISTIC)
+    plan.set_option(E.Plan.OPT_MSTEP_PAIR, pair)
+    plan.set_option(E.Plan.OPT_MSTEP_QLO, q_lo)
+    plan.set_option(E.Plan.OPT_MSTEP_RASTER, raster)
+    plan.bind(T(prob.images, dev), T(prob.mask, dev, torch.int32), T(prob.x, dev), T(prob.y, dev),
+              T(prob.z, dev), T(prob.quats, dev), T(prob.weights, dev))
+    m = T(prob.init_model, dev)
+    w = torch.empty_like(m)
+    st = plan.iterate(m, w, 0.3)
+    plan.close()
+    return m.cpu().numpy(), w.cpu().numpy(), st
+
+
+@pytest.mark.parametrize("q_lo", [0, 1])
+def test_mstep_pair_matches_single_cta(ctx, cuda, q_lo):
+    """The M-step on CTA pairs (EMC_OPT_MSTEP_PAIR) against single CTAs: an odd
+    number of 128-rotation tiles (the last pair's second CTA has no
+    rotations), a ragged pixel count, Q hi and Q hi + lo, two tile orders;
+    deterministic insertion, so equal sums give equal models."""
+    prob = S.make_problem(S.tiny(side=40, n_images=500, rot_n=3, photons=3000, n_atoms=120,
+                                 radius=8.0, seed=4))
+    R = prob.quats.shape[0]
+    assert ((R + 127) // 128) % 2 == 1
+    m1, w1, st1 = run_mstep(ctx, prob, cuda, 0, q_lo)
+    for raster in (-16, 3):
+        m2, w2, st2 = run_mstep(ctx, prob, cuda, 1, q_lo, raster)
+        np.testing.assert_allclose(w2, w1, rtol=1e-6, atol=1e-6 * np.abs(w1).max())
+        np.testing.assert_allclose(m2, m1, rtol=1e-5, atol=1e-6 * np.abs(m1).max())
+        assert abs(st2.total_loglik - st1.total_loglik) <= 1e-9 * abs(st1.total_loglik)

@@ -69,13 +69,15 @@ def parse():
                          "the large configuration, 0 otherwise)")
     ap.add_argument("--estep-pair", type=int, choices=[0, 1], default=1,
                     help="tensor path: full likelihood scans on CTA pairs (EMC_OPT_ESTEP_PAIR)")
-    ap.add_argument("--mstep-pair", type=int, choices=[0, 1], default=1,
+    ap.add_argument("--mstep-pair", type=int, choices=[0, 1], default=0,
                     help="tensor path: full-scan M-step on CTA pairs (EMC_OPT_MSTEP_PAIR)")
     ap.add_argument("--raster", type=int, default=0,
                     help="tensor path: the likelihood kernel's tile order (EMC_OPT_ESTEP_RASTER); "
                          "0 (default): chosen by emc_plan_autotune before the warm-up")
     ap.add_argument("--plain-steps", type=int, default=2)
-    ap.add_argument("--e2e-steps", type=int, default=4)
+    ap.add_argument("--e2e-steps", type=int, default=-1,
+                    help="end-to-end steps (-1: max(4, steps / 2)); the first step's pattern "
+                         "copy is not hidden, later ones overlap the previous step")
     ap.add_argument("--cpu-seconds", type=float, default=15.0,
                     help="target duration of the FP64 host-oracle baseline (cpu_baseline)")
     ap.add_argument("--ref-seconds", type=float, default=100.0,
@@ -89,6 +91,8 @@ def parse():
     args = ap.parse_args()
     if args.counts_round < 0:
         args.counts_round = int(args.config == "large")
+    if args.e2e_steps < 0:
+        args.e2e_steps = max(4, args.steps // 2)
     if args.learned_epochs < 0:
         args.learned_epochs = 30 if args.config == "large" else 0
     return args

@@ -118,8 +118,10 @@ __global__ void pattern_ops_kernel(const float* __restrict__ images, const int* 
     }
     k = __fmul_rn(v, __ldg(cnorm + i));
   }
-  double sum = (double)k;
-  for (int o = 16; o > 0; o >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, o);
+  // FP32 warp tree (exact for integer counts; FP64 throughput is scarce), FP64 after
+  float fsum = k;
+  for (int o = 16; o > 0; o >>= 1) fsum += __shfl_down_sync(0xffffffffu, fsum, o);
+  const double sum = (double)fsum;
   bits = __reduce_or_sync(0xffffffffu, (unsigned)bits);
   vmax = __reduce_max_sync(0xffffffffu, vmax);
   __shared__ double wsum[8];
@@ -169,9 +171,11 @@ __global__ void pattern_ops_kernel(const float* __restrict__ images, const int* 
 // pixel list's (radius) order -- the list scatters over the whole row, and
 // gathering it from global memory, one load per thread in flight, took 3.5 ms
 // of a 4.2 ms bind at 128^3 x 20,000 patterns.  For rows that fit shared
-// memory (pattern_row_smem <= kRowSmemMax).  Ksum[i] is written directly with
-// pattern_ops_kernel's arithmetic: per 256-pixel block a warp-shuffle tree
-// per 32 pixels, the 8 warp sums in order, then the blocks in order, in FP64.
+// memory (pattern_row_smem <= kRowSmemMax).  Ksum[i] is written directly: a
+// warp-shuffle tree per 32 pixels in FP32 (exact for integer counts, whose
+// sums stay below 2^24; FP64 arithmetic runs at a small fraction of the FP32
+// rate on this GPU, and an FP64 tree per pixel took as long as the rest of
+// the bind), then the warp sums in pixel order in FP64.
 constexpr int kRowThreads = 512;
 constexpr int kRowSmemMax = 200 * 1024;
 
@@ -218,9 +222,9 @@ __global__ void __launch_bounds__(kRowThreads) pattern_row_kernel(
       }
       k = __fmul_rn(v, ci);
     }
-    double sum = (double)k;
+    float sum = k;
     for (int o = 16; o > 0; o >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, o);
-    if (lane == 0 && q - lane < nqb * 256) wsum[(q - lane) / 32] = sum;
+    if (lane == 0 && q - lane < nqb * 256) wsum[(q - lane) / 32] = (double)sum;
     if (in) {
       const size_t o = (size_t)i * Kp + q;
       if (Kraw) Kraw[o] = k;
@@ -1841,6 +1845,11 @@ extern "C" int emc_plan_set_option(emc_plan* p, int option, int value) {
   if (option == EMC_OPT_ESTEP_PAIR) {
     EMC_REQUIRE(ctx, value == 0 || value == 1, "plan_set_option: pair %d", value);
     p->estep_pair = value;
+    return EMC_OK;
+  }
+  if (option == EMC_OPT_ESTEP_K2_ONCHIP) {
+    EMC_REQUIRE(ctx, value == 0 || value == 1, "plan_set_option: K^2 on chip %d", value);
+    p->estep_k2_onchip = value;
     return EMC_OK;
   }
   if (option == EMC_OPT_MSTEP_PAIR) {

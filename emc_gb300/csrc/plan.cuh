@@ -107,6 +107,7 @@ struct emc_plan {
   int mstep_q_lo = 0;     // tensor M-step: Q as FP16 hi + lo (1) or hi only (0)
   int estep_raster = 8;     // tensor E-step tile order (EMC_OPT_ESTEP_RASTER)
   int estep_pair = 1;       // full scans on CTA pairs (EMC_OPT_ESTEP_PAIR)
+  int estep_k2_onchip = 0;  // pair kernel forms K^2 in shared memory (EMC_OPT_ESTEP_K2_ONCHIP)
   int mstep_raster = -16;   // tensor M-step tile order (EMC_OPT_MSTEP_RASTER)
   int mstep_aggregate = 0;  // tensor M-step: warp-aggregated float atomics (nearest)
   unsigned debug_spin = 0;  // > 0: polls per tensor-pipeline wait (EMC_OPT_DEBUG_SPIN)

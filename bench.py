@@ -69,9 +69,6 @@ def parse():
                          "the large configuration, 0 otherwise)")
     ap.add_argument("--estep-pair", type=int, choices=[0, 1], default=1,
                     help="tensor path: full likelihood scans on CTA pairs (EMC_OPT_ESTEP_PAIR)")
-    ap.add_argument("--k2-onchip", type=int, choices=[0, 1], default=0,
-                    help="tensor path: the pair likelihood kernel forms K^2 in shared memory "
-                         "(EMC_OPT_ESTEP_K2_ONCHIP)")
     ap.add_argument("--mstep-pair", type=int, choices=[0, 1], default=0,
                     help="tensor path: full-scan M-step on CTA pairs (EMC_OPT_MSTEP_PAIR)")
     ap.add_argument("--raster", type=int, default=0,
@@ -313,7 +310,6 @@ def run_ours(args):
             p.set_option(E.Plan.OPT_COUNTS_ROUND, 1)
         p.set_option(E.Plan.OPT_ESTEP_PAIR, args.estep_pair)
         p.set_option(E.Plan.OPT_MSTEP_PAIR, args.mstep_pair)
-        p.set_option(E.Plan.OPT_ESTEP_K2_ONCHIP, args.k2_onchip)
         p.bind(images, mask, x, y, z, rot, w)
         return p
 

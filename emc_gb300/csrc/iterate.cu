@@ -172,7 +172,7 @@ __global__ void pattern_ops_kernel(const float* __restrict__ images, const int* 
 // gathering it from global memory, one load per thread in flight, took 3.5 ms
 // of a 4.2 ms bind at 128^3 x 20,000 patterns.  For rows that fit shared
 // memory (pattern_row_smem <= kRowSmemMax).  Ksum[i] is written directly: a
-// warp-shuffle tree per 32 pixels in FP32 (exact for integer counts, whose
+// warp-shuffle tree per 64 pixels in FP32 (exact for integer counts, whose
 // sums stay below 2^24; FP64 arithmetic runs at a small fraction of the FP32
 // rate on this GPU, and an FP64 tree per pixel took as long as the rest of
 // the bind), then the warp sums in pixel order in FP64.
@@ -204,43 +204,52 @@ __global__ void __launch_bounds__(kRowThreads) pattern_row_kernel(
   }
   __syncthreads();
   const float ci = __ldg(cnorm + i);
-  const int nqb = (Kp + 255) / 256;
   int bits = 0, vmax = 0;
-  for (int q0 = 0; q0 < nqb * 256; q0 += blockDim.x) {
-    const int q = q0 + threadIdx.x;
-    const bool in = q < Kp;
-    const int p = in ? __ldg(pix + q) : -1;
-    float v = 0.0f, k = 0.0f;
-    if (p >= 0) {
-      v = srow[p];
-      if (!isfinite(v)) bits |= 1;
-      if (!(v >= 0.0f && v <= 65504.0f && v == rintf(v))) {
-        bits |= 2;
-      } else {
-        if (v > 2048.0f) bits |= 8;
-        vmax = max(vmax, (int)v);
-      }
-      k = __fmul_rn(v, ci);
-    }
-    float sum = k;
-    for (int o = 16; o > 0; o >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, o);
-    if (lane == 0 && q - lane < nqb * 256) wsum[(q - lane) / 32] = (double)sum;
-    if (in) {
-      const size_t o = (size_t)i * Kp + q;
-      if (Kraw) Kraw[o] = k;
-      const float kt = k >= 1e-10f ? k : 0.0f;  // the reference's (double)k > 1e-10
-      if (Kt) Kt[o] = kt;
-      if (K2) K2[o] = __fmul_rn(kt, kt);
-      if (Kh) {
-        const __half kh = __float2half_rn(v);
-        const float kr = __half2float(kh);
-        const float k2 = kr * kr * k2_scale;
-        const __half hi = __float2half_rn(k2);
-        Kh[o] = kh;
-        if (K2h) {
-          K2h[o] = hi;
-          K2l[o] = __float2half_rn(k2 - __half2float(hi));
+  // two neighbouring pixels per thread (Kp is a multiple of 128): the
+  // compacted operands go out as 8-byte (float2) and 4-byte (half2) stores
+  for (int q = 2 * threadIdx.x; q < Kp; q += 2 * blockDim.x) {
+    const int2 pp = __ldg(reinterpret_cast<const int2*>(pix + q));
+    const int pv[2] = {pp.x, pp.y};
+    float v[2], k[2];
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      v[u] = 0.0f;
+      k[u] = 0.0f;
+      if (pv[u] >= 0) {
+        v[u] = srow[pv[u]];
+        if (!isfinite(v[u])) bits |= 1;
+        if (!(v[u] >= 0.0f && v[u] <= 65504.0f && v[u] == rintf(v[u]))) {
+          bits |= 2;
+        } else {
+          if (v[u] > 2048.0f) bits |= 8;
+          vmax = max(vmax, (int)v[u]);
         }
+        k[u] = __fmul_rn(v[u], ci);
+      }
+    }
+    float sum = k[0] + k[1];
+    for (int o = 16; o > 0; o >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, o);
+    if (lane == 0) wsum[(q - 2 * lane) / 64] = (double)sum;
+    const size_t o = (size_t)i * Kp + q;
+    if (Kraw) *reinterpret_cast<float2*>(Kraw + o) = make_float2(k[0], k[1]);
+    const float kt0 = k[0] >= 1e-10f ? k[0] : 0.0f;  // the reference's (double)k > 1e-10
+    const float kt1 = k[1] >= 1e-10f ? k[1] : 0.0f;
+    if (Kt) *reinterpret_cast<float2*>(Kt + o) = make_float2(kt0, kt1);
+    if (K2) *reinterpret_cast<float2*>(K2 + o) = make_float2(__fmul_rn(kt0, kt0), __fmul_rn(kt1, kt1));
+    if (Kh) {
+      __half kh[2], hi[2], lw[2];
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+        kh[u] = __float2half_rn(v[u]);
+        const float kr = __half2float(kh[u]);
+        const float k2 = kr * kr * k2_scale;
+        hi[u] = __float2half_rn(k2);
+        lw[u] = __float2half_rn(k2 - __half2float(hi[u]));
+      }
+      *reinterpret_cast<__half2*>(Kh + o) = __halves2half2(kh[0], kh[1]);
+      if (K2h) {
+        *reinterpret_cast<__half2*>(K2h + o) = __halves2half2(hi[0], hi[1]);
+        *reinterpret_cast<__half2*>(K2l + o) = __halves2half2(lw[0], lw[1]);
       }
     }
   }
@@ -254,11 +263,7 @@ __global__ void __launch_bounds__(kRowThreads) pattern_row_kernel(
   __syncthreads();
   if (threadIdx.x == 0) {
     double s = 0.0;
-    for (int b = 0; b < nqb; ++b) {
-      double t = 0.0;
-      for (int w = 0; w < 8; ++w) t += wsum[b * 8 + w];
-      s += t;
-    }
+    for (int w = 0; w < Kp / 64; ++w) s += wsum[w];
     Ksum[i] = (float)s;
     int bb = 0, m = 0;
     for (int w = 0; w < (int)(blockDim.x / 32); ++w) {
@@ -342,22 +347,37 @@ __global__ void __launch_bounds__(256) slice_rows_kernel(
   const RotMat Rm = sR;
   // per-thread FP32 partials (FP64 arithmetic is scarce on this GPU), block sums in FP64
   float cnt = 0.0f, A = 0.0f, ss = 0.0f;
-  for (int q = threadIdx.x; q < Kp; q += blockDim.x) {
-    float s = 0.0f;
-    if (__ldg(pix + q) >= 0) {
-      s = plan_sample<INTERP>(model, side, Rm, __ldg(cx + q), __ldg(cy + q), __ldg(cz + q));
-      if (s > 0.0f) {
+  // two neighbouring pixels per thread and pass (Kp is a multiple of 128):
+  // their coordinates in 8-byte loads and the tensor path's six operand
+  // planes in 4-byte stores
+  for (int q = 2 * threadIdx.x; q < Kp; q += 2 * blockDim.x) {
+    const int2 pp = __ldg(reinterpret_cast<const int2*>(pix + q));
+    const float2 X = __ldg(reinterpret_cast<const float2*>(cx + q));
+    const float2 Y = __ldg(reinterpret_cast<const float2*>(cy + q));
+    const float2 Z = __ldg(reinterpret_cast<const float2*>(cz + q));
+    const float s0 = pp.x >= 0 ? plan_sample<INTERP>(model, side, Rm, X.x, Y.x, Z.x) : 0.0f;
+    const float s1 = pp.y >= 0 ? plan_sample<INTERP>(model, side, Rm, X.y, Y.y, Z.y) : 0.0f;
+    if (pp.x >= 0) {
+      if (s0 > 0.0f) {
         cnt += 1.0f;
-        A += s * s / (s + kPoisC);
+        A += s0 * s0 / (s0 + kPoisC);
       }
-      ss += fmaxf(s, kSliceFloor);
+      ss += fmaxf(s0, kSliceFloor);
+    }
+    if (pp.y >= 0) {
+      if (s1 > 0.0f) {
+        cnt += 1.0f;
+        A += s1 * s1 / (s1 + kPoisC);
+      }
+      ss += fmaxf(s1, kSliceFloor);
     }
     // the tensor path takes its FP16 operands straight from s; the FP32 path
     // keeps the slices
+    const size_t e = (size_t)r * Kp + q;
     if (ops.Gh)
-      rot_ops_store(ops, (size_t)r * Kp + q, s);
+      rot_ops_store2(ops, e, s0, s1);
     else
-      S[(size_t)r * Kp + q] = s;
+      *reinterpret_cast<float2*>(S + e) = make_float2(s0, s1);
   }
   __shared__ double sh[3][256];
   sh[0][threadIdx.x] = (double)cnt;
@@ -821,30 +841,54 @@ __global__ void __launch_bounds__(kMprepThreads) mprep_kernel(
   }
   if (Q)
     for (int i = N + threadIdx.x; i < ldq; i += blockDim.x) Q[(size_t)r * ldq + i] = 0.0f;
-  __shared__ double sh[3][kMprepThreads];
-  __shared__ float smx[kMprepThreads];
-  sh[0][threadIdx.x] = (double)t;
-  sh[1][threadIdx.x] = (double)b;
-  sh[2][threadIdx.x] = (double)mg;
-  smx[threadIdx.x] = qmax;
-  __syncthreads();
-  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-    if (threadIdx.x < o) {
-      sh[0][threadIdx.x] += sh[0][threadIdx.x + o];
-      sh[1][threadIdx.x] += sh[1][threadIdx.x + o];
-      sh[2][threadIdx.x] += sh[2][threadIdx.x + o];
-      smx[threadIdx.x] = fmaxf(smx[threadIdx.x], smx[threadIdx.x + o]);
-    }
-    __syncthreads();
+  // row sums and maximum: FP32 warp shuffles over the threads' FP32
+  // partials, then the 32 warp sums in FP64 on warp 0 -- a block tree over
+  // 1,024 shared FP64 slots took 28 KB of shared memory (one block per SM
+  // with the staged row) and ten block barriers, and FP64 shuffles in every
+  // warp cost more than they saved (FP64 runs at a small fraction of the
+  // FP32 rate on this GPU)
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  float f0 = t, f1 = b, f2 = mg, rmx = qmax;
+  for (int o = 16; o > 0; o >>= 1) {
+    f0 += __shfl_down_sync(0xffffffffu, f0, o);
+    f1 += __shfl_down_sync(0xffffffffu, f1, o);
+    f2 += __shfl_down_sync(0xffffffffu, f2, o);
+    rmx = fmaxf(rmx, __shfl_down_sync(0xffffffffu, rmx, o));
   }
-  if (threadIdx.x == 0) {
-    T[r] = (float)sh[0][0];
-    row_mass[r] = sh[0][0];
-    row_bound[r] = sh[1][0];
-    if (row_margin) row_margin[r] = sh[2][0];
+  double r0s = (double)f0, r1s = (double)f1, r2s = (double)f2;
+  __shared__ double wsum[3][kMprepThreads / 32];
+  __shared__ float wmax[kMprepThreads / 32];
+  __shared__ float row_max;
+  if (lane == 0) {
+    wsum[0][warp] = r0s;
+    wsum[1][warp] = r1s;
+    wsum[2][warp] = r2s;
+    wmax[warp] = rmx;
+  }
+  __syncthreads();
+  if (warp == 0) {
+    const int nw = (int)(blockDim.x >> 5);
+    r0s = lane < nw ? wsum[0][lane] : 0.0;
+    r1s = lane < nw ? wsum[1][lane] : 0.0;
+    r2s = lane < nw ? wsum[2][lane] : 0.0;
+    rmx = lane < nw ? wmax[lane] : 0.0f;
+    for (int o = 16; o > 0; o >>= 1) {
+      r0s += __shfl_down_sync(0xffffffffu, r0s, o);
+      r1s += __shfl_down_sync(0xffffffffu, r1s, o);
+      r2s += __shfl_down_sync(0xffffffffu, r2s, o);
+      rmx = fmaxf(rmx, __shfl_down_sync(0xffffffffu, rmx, o));
+    }
+    if (lane == 0) {
+      T[r] = (float)r0s;
+      row_mass[r] = r0s;
+      row_bound[r] = r1s;
+      if (row_margin) row_margin[r] = r2s;
+      row_max = rmx;
+    }
   }
   if (!Qh) return;
-  const float mx = smx[0];
+  __syncthreads();
+  const float mx = row_max;
   int ex = mx > 0.0f ? 14 - ilogbf(mx) - 1 : 0;
   ex = max(-100, min(100, ex));
   const float up = ldexpf(1.0f, ex);
@@ -1845,11 +1889,6 @@ extern "C" int emc_plan_set_option(emc_plan* p, int option, int value) {
   if (option == EMC_OPT_ESTEP_PAIR) {
     EMC_REQUIRE(ctx, value == 0 || value == 1, "plan_set_option: pair %d", value);
     p->estep_pair = value;
-    return EMC_OK;
-  }
-  if (option == EMC_OPT_ESTEP_K2_ONCHIP) {
-    EMC_REQUIRE(ctx, value == 0 || value == 1, "plan_set_option: K^2 on chip %d", value);
-    p->estep_k2_onchip = value;
     return EMC_OK;
   }
   if (option == EMC_OPT_MSTEP_PAIR) {

@@ -107,7 +107,6 @@ struct emc_plan {
   int mstep_q_lo = 0;     // tensor M-step: Q as FP16 hi + lo (1) or hi only (0)
   int estep_raster = 8;     // tensor E-step tile order (EMC_OPT_ESTEP_RASTER)
   int estep_pair = 1;       // full scans on CTA pairs (EMC_OPT_ESTEP_PAIR)
-  int estep_k2_onchip = 0;  // pair kernel forms K^2 in shared memory (EMC_OPT_ESTEP_K2_ONCHIP)
   int mstep_raster = -16;   // tensor M-step tile order (EMC_OPT_MSTEP_RASTER)
   int mstep_aggregate = 0;  // tensor M-step: warp-aggregated float atomics (nearest)
   unsigned debug_spin = 0;  // > 0: polls per tensor-pipeline wait (EMC_OPT_DEBUG_SPIN)
@@ -173,9 +172,54 @@ __device__ __forceinline__ void rot_ops_store(const RotOps& o, size_t e, float s
   o.Mp[e] = __float2half_rn(mp ? 1.0f : 0.0f);
   o.MSh[e] = __float2half_rn(ms);
   o.Gh[e] = gh;
-  o.Gl[e] = __float2half_rn(g - __half2float(gh));
+  if (o.Gl) o.Gl[e] = __float2half_rn(g - __half2float(gh));
   o.Hh[e] = hh;
-  o.Hl[e] = __float2half_rn(h - __half2float(hh));
+  if (o.Hl) o.Hl[e] = __float2half_rn(h - __half2float(hh));
+}
+
+// The operands of two neighbouring pixels e, e + 1 (e even) as 4-byte stores.
+__device__ __forceinline__ void rot_ops_store2(const RotOps& o, size_t e, float s0, float s1) {
+  const float sv[2] = {s0, s1};
+  if (o.logs) {
+    __half2 hi, lo;
+    __half* ph = reinterpret_cast<__half*>(&hi);
+    __half* pl = reinterpret_cast<__half*>(&lo);
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      const float l = logf(fmaxf(sv[u], 1e-6f));
+      ph[u] = __float2half_rn(l);
+      pl[u] = __float2half_rn(l - __half2float(ph[u]));
+    }
+    *reinterpret_cast<__half2*>(o.Gh + e) = hi;
+    *reinterpret_cast<__half2*>(o.Gl + e) = lo;
+    return;
+  }
+  __half2 mp2, ms2, gh2, gl2, hh2, hl2;
+  __half *pmp = reinterpret_cast<__half*>(&mp2), *pms = reinterpret_cast<__half*>(&ms2),
+         *pgh = reinterpret_cast<__half*>(&gh2), *pgl = reinterpret_cast<__half*>(&gl2),
+         *phh = reinterpret_cast<__half*>(&hh2), *phl = reinterpret_cast<__half*>(&hl2);
+#pragma unroll
+  for (int u = 0; u < 2; ++u) {
+    const float s = sv[u];
+    const bool mp = s >= 1e-10f;
+    const bool m = s > 0.0f;
+    const float ms = mp ? s * (1.0f / 256.0f) : 0.0f;
+    if (ms > 60000.0f) atomicOr(o.flags, 4);
+    const float h = m ? 1.0f / (s + 0.02f) : 0.0f;
+    const float g = m ? s * h : 0.0f;
+    pmp[u] = __float2half_rn(mp ? 1.0f : 0.0f);
+    pms[u] = __float2half_rn(ms);
+    pgh[u] = __float2half_rn(g);
+    pgl[u] = __float2half_rn(g - __half2float(pgh[u]));
+    phh[u] = __float2half_rn(h);
+    phl[u] = __float2half_rn(h - __half2float(phh[u]));
+  }
+  *reinterpret_cast<__half2*>(o.Mp + e) = mp2;
+  *reinterpret_cast<__half2*>(o.MSh + e) = ms2;
+  *reinterpret_cast<__half2*>(o.Gh + e) = gh2;
+  if (o.Gl) *reinterpret_cast<__half2*>(o.Gl + e) = gl2;
+  *reinterpret_cast<__half2*>(o.Hh + e) = hh2;
+  if (o.Hl) *reinterpret_cast<__half2*>(o.Hl + e) = hl2;
 }
 
 RotOps tc_rot_ops(emc_plan* p);  // the plan's operand buffers (all null for FP32 plans)

@@ -129,19 +129,39 @@ __global__ void tc_k2lo_flags_kernel(const __half* __restrict__ K2l, int Kp,
   if (threadIdx.x == 0) flags[(size_t)pt * nkb + kb] = (unsigned char)any;
 }
 
-// [rows][cols] -> [cols][rows], FP16, 32x32 tiles.
+// [rows][cols] -> [cols][rows], FP16: 64 x 64 tiles, moved with 4-byte
+// (half2) loads and stores where two neighbouring elements are in range.
 __global__ void transpose_h_kernel(const __half* __restrict__ in, int rows, int cols,
                                    __half* __restrict__ out) {
-  __shared__ __half t[32][33];
-  const int c0 = blockIdx.x * 32, r0 = blockIdx.y * 32;
-  for (int y = threadIdx.y; y < 32; y += blockDim.y) {
-    const int r = r0 + y, c = c0 + threadIdx.x;
-    t[y][threadIdx.x] = (r < rows && c < cols) ? in[(size_t)r * cols + c] : __float2half_rn(0.f);
+  __shared__ __half t[64][66];
+  const int c0 = blockIdx.x * 64, r0 = blockIdx.y * 64;
+  const int x2 = 2 * threadIdx.x;
+  for (int y = threadIdx.y; y < 64; y += blockDim.y) {
+    const int r = r0 + y, c = c0 + x2;
+    __half a = __float2half_rn(0.f), b = a;
+    if (r < rows) {
+      if (c + 1 < cols && (cols & 1) == 0) {
+        const __half2 v = *reinterpret_cast<const __half2*>(in + (size_t)r * cols + c);
+        a = __low2half(v);
+        b = __high2half(v);
+      } else {
+        if (c < cols) a = in[(size_t)r * cols + c];
+        if (c + 1 < cols) b = in[(size_t)r * cols + c + 1];
+      }
+    }
+    t[y][x2] = a;
+    t[y][x2 + 1] = b;
   }
   __syncthreads();
-  for (int y = threadIdx.y; y < 32; y += blockDim.y) {
-    const int c = c0 + y, r = r0 + threadIdx.x;
-    if (c < cols && r < rows) out[(size_t)c * rows + r] = t[threadIdx.x][y];
+  for (int y = threadIdx.y; y < 64; y += blockDim.y) {
+    const int c = c0 + y, r = r0 + x2;
+    if (c >= cols) continue;
+    if (r + 1 < rows && (rows & 1) == 0) {
+      *reinterpret_cast<__half2*>(out + (size_t)c * rows + r) = __halves2half2(t[x2][y], t[x2 + 1][y]);
+    } else {
+      if (r < rows) out[(size_t)c * rows + r] = t[x2][y];
+      if (r + 1 < rows) out[(size_t)c * rows + r + 1] = t[x2 + 1][y];
+    }
   }
 }
 
@@ -205,7 +225,6 @@ struct TcEstepArgs {
   const float* rotw;
   const float* cnorm;   // c_i (phi is stored as c_i num/den)
   float k2_inv;         // 1 / k2_scale of the K^2 operand
-  float k2_scale;       // the K^2 operand's scale (on-chip K^2)
   const float* sigma;   // [1] annealing width (device memory)
   int known_intensity;
   float* L;
@@ -214,7 +233,6 @@ struct TcEstepArgs {
   int* bad;
   int* status;
   uint32_t spin;  // polls per pipeline wait (ptx::kSpinLimit unless a debug option lowers it)
-  int k2_onchip;  // pair kernel: form K^2 hi / lo from the K tile in shared memory
 };
 
 // Epilogue of the likelihood kernels (warps 2 .. 2 + EPI_WARPS - 1): EPI_PARTS
@@ -444,7 +462,6 @@ constexpr int HALF = TILE / 2;          // 64 rows (G lo half)
 constexpr int oK = 0, oK2h = TILE, oK2l = 2 * TILE, oB1 = 3 * TILE, oB2 = 4 * TILE,
               oGl = 5 * TILE;
 constexpr int STAGE_BYTES = 5 * TILE + HALF;  // 44 KB; no H lo (known intensity runs single CTAs)
-constexpr int kConvWarps = 4;  // epilogue warps that form K^2 on chip during the k-loop
 // barriers (256 B), per-rotation rows (3 x 128 floats), epilogue parts
 constexpr int EXTRA = 256 + 3 * es::BN * 4 + (es::EPI_PARTS - 1) * es::BM * 8;
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + EXTRA + 1024;
@@ -469,9 +486,7 @@ __global__ void __launch_bounds__(es::THREADS, 1)
   uint64_t* empty = full + STAGES;
   uint64_t* accum = empty + STAGES;
   uint64_t* drain = accum + 1;  // rank 0's MMA issuer waits on it before TMEM is freed
-  uint64_t* kfull = drain + 1;   // [STAGES] on-chip K^2: this CTA's K tile landed
-  uint64_t* k2ready = kfull + STAGES;  // [STAGES] rank 0: both CTAs' K^2 tiles written
-  uint32_t* tmem_slot = (uint32_t*)(k2ready + STAGES);
+  uint32_t* tmem_slot = (uint32_t*)(drain + 1);
   float* s_A = (float*)(smem + STAGES * STAGE_BYTES + 256);
   float* s_scale = s_A + BN;
   float* s_lw = s_scale + BN;
@@ -491,8 +506,6 @@ __global__ void __launch_bounds__(es::THREADS, 1)
     for (int s = 0; s < STAGES; ++s) {
       ptx::mbar_init(&full[s], 1);
       ptx::mbar_init(&empty[s], 1);
-      ptx::mbar_init(&kfull[s], 1);
-      ptx::mbar_init(&k2ready[s], 2 * es2::kConvWarps);
     }
     ptx::mbar_init(accum, 1);
     ptx::mbar_init(drain, 1);
@@ -531,23 +544,14 @@ __global__ void __launch_bounds__(es::THREADS, 1)
         const uint32_t ph = (kb / STAGES) & 1;
         if (!ptx::mbar_wait(&empty[s], ph ^ 1, a.status, 0, a.spin)) break;
         const bool lo = flags0[kb] != 0 || (flags1 && flags1[kb] != 0);
+        const uint32_t bytes = (lo ? 5 : 4) * es2::TILE + (glo ? es2::HALF : 0);
+        if (rank == 0) ptx::mbar_arrive_expect_tx(&full[s], 2 * bytes);  // both CTAs' loads
         const uint32_t fb = ptx::mapa_shared(ptx::smem_u32(&full[s]), 0);
         unsigned char* st = smem + s * STAGE_BYTES;
         const int x = kb * BK;
-        if (a.k2_onchip) {
-          // K lands on this CTA's own kfull[s]; the converter warps form K^2
-          // from it, and rank 0's full[s] counts the rotation tiles only
-          const uint32_t bytes = 2 * es2::TILE + (glo ? es2::HALF : 0);
-          if (rank == 0) ptx::mbar_arrive_expect_tx(&full[s], 2 * bytes);
-          ptx::mbar_arrive_expect_tx(&kfull[s], es2::TILE);
-          ptx::tma_load_2d(st + es2::oK, &mK, x, n0, &kfull[s]);
-        } else {
-          const uint32_t bytes = (lo ? 5 : 4) * es2::TILE + (glo ? es2::HALF : 0);
-          if (rank == 0) ptx::mbar_arrive_expect_tx(&full[s], 2 * bytes);  // both CTAs' loads
-          ptx::tma_load_2d_pair(st + es2::oK, &mK, x, n0, fb);
-          ptx::tma_load_2d_pair(st + es2::oK2h, &mK2h, x, n0, fb);
-          if (lo) ptx::tma_load_2d_pair(st + es2::oK2l, &mK2l, x, n0, fb);
-        }
+        ptx::tma_load_2d_pair(st + es2::oK, &mK, x, n0, fb);
+        ptx::tma_load_2d_pair(st + es2::oK2h, &mK2h, x, n0, fb);
+        if (lo) ptx::tma_load_2d_pair(st + es2::oK2l, &mK2l, x, n0, fb);
         ptx::tma_load_2d_pair(st + es2::oB1, mb1, x, r0, fb);
         ptx::tma_load_2d_pair(st + es2::oB2, mb2, x, r0, fb);
         if (glo) ptx::tma_load_2d_pair(st + es2::oGl, &mGl64, x, r0 + 64 * (int)rank, fb);
@@ -564,8 +568,6 @@ __global__ void __launch_bounds__(es::THREADS, 1)
         const int s = kb % STAGES;
         const uint32_t ph = (kb / STAGES) & 1;
         if (!ptx::mbar_wait(&full[s], ph, a.status, 1, a.spin)) break;
-        // on-chip K^2: both CTAs' converter warps arrive remotely (cluster scope)
-        if (a.k2_onchip && !ptx::mbar_wait_cluster(&k2ready[s], ph, a.status, 14, a.spin)) break;
         ptx::tc_fence_after();
         const bool lo = flags0[kb] != 0 || (flags1 && flags1[kb] != 0);
         const uint32_t base = ptx::smem_u32(smem + s * STAGE_BYTES);
@@ -585,44 +587,6 @@ __global__ void __launch_bounds__(es::THREADS, 1)
       ptx::mbar_wait(drain, 0, a.status, 12);
     }
   } else {
-    if (a.k2_onchip && warp < 2 + es2::kConvWarps) {
-      // ---------------------------------------- K^2 converter (warps 2..)
-      // idle until the tile's epilogue: forms K^2 x k2_scale as FP16 hi (+ lo
-      // in flagged k-blocks) from each landed K tile, element by element in
-      // place of the tiles that would otherwise be streamed from L2 (the
-      // likelihood's stages are bound by that stream), with the bind's
-      // arithmetic, so the operands are the same bits
-      const int t = (warp - 2) * 32 + lane;
-      const uint32_t kr_bar = ptx::mapa_shared(ptx::smem_u32(&k2ready[0]), 0);
-      for (int kb = 0; kb < a.nkb; ++kb) {
-        const int s = kb % STAGES;
-        const uint32_t ph = (kb / STAGES) & 1;
-        if (!ptx::mbar_wait(&kfull[s], ph, a.status, 15, a.spin)) break;
-        const bool lo = flags0[kb] != 0 || (flags1 && flags1[kb] != 0);
-        unsigned char* st = smem + s * STAGE_BYTES;
-        const uint4* src = reinterpret_cast<const uint4*>(st + es2::oK);
-        uint4* dh = reinterpret_cast<uint4*>(st + es2::oK2h);
-        uint4* dl = reinterpret_cast<uint4*>(st + es2::oK2l);
-        for (int v = t; v < es2::TILE / 16; v += 32 * es2::kConvWarps) {
-          uint4 in = src[v], hi, lw;
-          const __half* hin = reinterpret_cast<const __half*>(&in);
-          __half* hh = reinterpret_cast<__half*>(&hi);
-          __half* hl = reinterpret_cast<__half*>(&lw);
-#pragma unroll
-          for (int e = 0; e < 8; ++e) {
-            const float kr = __half2float(hin[e]);
-            const float k2 = kr * kr * a.k2_scale;
-            hh[e] = __float2half_rn(k2);
-            hl[e] = __float2half_rn(k2 - __half2float(hh[e]));
-          }
-          dh[v] = hi;
-          if (lo) dl[v] = lw;
-        }
-        ptx::fence_proxy_async_smem();  // visible to the tensor core's reads
-        __syncwarp();
-        if (lane == 0) ptx::mbar_arrive_cluster(kr_bar + (uint32_t)(s * sizeof(uint64_t)));
-      }
-    }
     // ------------------------------------------------ epilogue (warps 2-17)
     estep_epilogue(a, tmem, accum, s_A, s_scale, s_lw, s_half, warp, lane, n0, r0, rt);
   }
@@ -1406,7 +1370,7 @@ int tc_pattern_side(emc_plan* p, const int* d_perm, bool counts_done) {
   if (!pois) tc_k2lo_flags_kernel<<<dim3(Kp / 32, Np / 128), 256, 0, ctx->stream>>>(p->K2lo, Kp, p->k2lo_any,
                                                                          Kp / 32);
   if ((rc = after_launch(ctx, "tc_k2lo_flags_kernel"))) return rc;
-  transpose_h_kernel<<<dim3(ceil_div(Kp, 32), ceil_div(Np, 32)), dim3(32, 8), 0, ctx->stream>>>(
+  transpose_h_kernel<<<dim3(ceil_div(Kp, 64), ceil_div(Np, 64)), dim3(32, 8), 0, ctx->stream>>>(
       p->Kh, Np, Kp, p->KhT);
   return after_launch(ctx, "transpose_h_kernel");
 }
@@ -1478,8 +1442,6 @@ static int estep_launch(emc_plan* p, int raster, int first, int count, bool full
   a.tiles = full ? nullptr : p->prune_tiles;
   a.k2lo_any = p->k2lo_any;
   a.k2_inv = 1.0f / p->k2_scale;
-  a.k2_scale = p->k2_scale;
-  a.k2_onchip = p->estep_k2_onchip;
   a.rot_cnt = p->rot_cnt;
   a.rot_A = p->rot_A;
   a.rotw = p->rotw;
@@ -1547,10 +1509,14 @@ RotOps tc_rot_ops(emc_plan* p) {
   if (p->d.diff == EMC_DIFF_TRUE_POISSON) {
     o.logs = 1;
   } else {
+    // the lo planes only where the likelihood reads them (EMC_OPT_ESTEP_GHLO;
+    // auto: G lo, and H lo when the intensity is known)
+    const int gh = p->estep_gh_lo >= 0 ? p->estep_gh_lo : (p->d.known_intensity ? 3 : 1);
     o.Mp = st->Mp;
     o.MSh = st->MSh;
     o.Hh = st->Hh;
-    o.Hl = st->Hl;
+    o.Gl = (gh & 1) ? st->Gl : nullptr;
+    o.Hl = (gh & 2) ? st->Hl : nullptr;
   }
   return o;
 }

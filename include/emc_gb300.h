@@ -487,14 +487,6 @@ int emc_batch_destroy(emc_batch* batch);
  * where a cluster launch is refused the plan falls back to single CTAs.
  * Results do not depend on it (bit for bit with deterministic insertion). */
 #define EMC_OPT_MSTEP_PAIR 10
-/* EMC_OPT_ESTEP_K2_ONCHIP: 1 makes the CTA-pair likelihood kernel form its
- * K^2 operand tiles (FP16 hi, and lo where needed) from the K tiles already
- * in shared memory, on warps that are idle until the tile's epilogue,
- * instead of streaming them from L2 (the kernel's stages are bound by that
- * stream: 28 instead of 36 KB per CTA and stage).  Same operand bits, same
- * results.  0: streamed.  Single-CTA and pruned likelihood scans always
- * stream them. */
-#define EMC_OPT_ESTEP_K2_ONCHIP 11
 int emc_plan_set_option(emc_plan* plan, int option, int value);
 /* Tile-order autotuner of the tensor-core likelihood kernel: expands d_model
  * (sigma as in emc_iterate), times the kernel for each candidate

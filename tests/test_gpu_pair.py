@@ -21,11 +21,10 @@ def T(a, dev, dt=torch.float32):
     return torch.as_tensor(np.ascontiguousarray(a), dtype=dt, device=dev)
 
 
-def run(ctx, prob, dev, pair, raster=8, k2=0, **kw):
+def run(ctx, prob, dev, pair, raster=8, **kw):
     s, R, N = prob.cfg.side, prob.quats.shape[0], prob.images.shape[0]
     plan = E.Plan(ctx, s, N, R, precision=E.PREC_MIXED, insert_mode=E.INSERT_DETERMINISTIC, **kw)
     plan.set_option(E.Plan.OPT_ESTEP_PAIR, pair)
-    plan.set_option(E.Plan.OPT_ESTEP_K2_ONCHIP, k2)
     plan.bind(T(prob.images, dev), T(prob.mask, dev, torch.int32), T(prob.x, dev), T(prob.y, dev),
               T(prob.z, dev), T(prob.quats, dev), T(prob.weights, dev))
     plan.set_option(E.Plan.OPT_ESTEP_RASTER, raster)
@@ -57,9 +56,8 @@ def test_pair_matches_single_cta(ctx, cuda, case):
     if case == "odd_tiles":
         assert prob.images.max() > 45  # K^2 lo blocks are used
     m1, L1, p1, st1 = run(ctx, prob, cuda, 0, **plan_kw)
-    # K^2 streamed from L2 or formed on chip (EMC_OPT_ESTEP_K2_ONCHIP): same operand bits
-    for raster, k2 in ((8, 0), (-19, 0), (2, 0), (8, 1), (-19, 1)):
-        m2, L2, p2, st2 = run(ctx, prob, cuda, 1, raster, k2, **plan_kw)
+    for raster in (8, -19, 2):
+        m2, L2, p2, st2 = run(ctx, prob, cuda, 1, raster, **plan_kw)
         ok = np.isfinite(L1)
         assert np.array_equal(ok, np.isfinite(L2))
         assert np.abs(L2[ok] - L1[ok]).max() <= 1e-6 * max(1.0, np.abs(L1[ok]).max())

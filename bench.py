@@ -66,7 +66,7 @@ def parse():
                          "(FP16 counts by its definition), off otherwise")
     ap.add_argument("--learned-epochs", type=int, default=-1,
                     help="learned rotation proposal leg: training epochs (0: skip; -1: 30 for "
-                         "the large configuration, 0 otherwise)")
+                         "the large configuration, 10 for mid, 0 otherwise)")
     ap.add_argument("--estep-pair", type=int, choices=[0, 1], default=1,
                     help="tensor path: full likelihood scans on CTA pairs (EMC_OPT_ESTEP_PAIR)")
     ap.add_argument("--mstep-pair", type=int, choices=[0, 1], default=0,
@@ -94,7 +94,7 @@ def parse():
     if args.e2e_steps < 0:
         args.e2e_steps = max(4, args.steps // 2)
     if args.learned_epochs < 0:
-        args.learned_epochs = 30 if args.config == "large" else 0
+        args.learned_epochs = {"large": 30, "mid": 10}.get(args.config, 0)
     return args
 
 

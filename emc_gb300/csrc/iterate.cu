@@ -297,9 +297,9 @@ template <>
 __device__ __forceinline__ float plan_sample<EMC_INTERP_NEAREST>(const float* __restrict__ model,
                                                                   int side, const RotMat& R,
                                                                   float x, float y, float z) {
-  const long ix = lroundf(voxel_coord(side, rotate_row(R, 0, x, y, z)));
-  const long iy = lroundf(voxel_coord(side, rotate_row(R, 1, x, y, z)));
-  const long iz = lroundf(voxel_coord(side, rotate_row(R, 2, x, y, z)));
+  const long ix = voxel_round(voxel_coord(side, rotate_row(R, 0, x, y, z)));
+  const long iy = voxel_round(voxel_coord(side, rotate_row(R, 1, x, y, z)));
+  const long iz = voxel_round(voxel_coord(side, rotate_row(R, 2, x, y, z)));
   if (ix > 0 && ix < side && iy > 0 && iy < side && iz > 0 && iz < side)
     return __ldg(model + ((size_t)iz * side + iy) * side + ix);
   return -1.0f;
@@ -357,17 +357,20 @@ __global__ void __launch_bounds__(256) slice_rows_kernel(
     const float2 Z = __ldg(reinterpret_cast<const float2*>(cz + q));
     const float s0 = pp.x >= 0 ? plan_sample<INTERP>(model, side, Rm, X.x, Y.x, Z.x) : 0.0f;
     const float s1 = pp.y >= 0 ? plan_sample<INTERP>(model, side, Rm, X.y, Y.y, Z.y) : 0.0f;
+    // one division per pixel: h = 1 / (s + c) serves A = s^2 h and the operands
+    const float h0 = s0 > 0.0f ? 1.0f / (s0 + kPoisC) : 0.0f;
+    const float h1 = s1 > 0.0f ? 1.0f / (s1 + kPoisC) : 0.0f;
     if (pp.x >= 0) {
       if (s0 > 0.0f) {
         cnt += 1.0f;
-        A += s0 * s0 / (s0 + kPoisC);
+        A += s0 * s0 * h0;
       }
       ss += fmaxf(s0, kSliceFloor);
     }
     if (pp.y >= 0) {
       if (s1 > 0.0f) {
         cnt += 1.0f;
-        A += s1 * s1 / (s1 + kPoisC);
+        A += s1 * s1 * h1;
       }
       ss += fmaxf(s1, kSliceFloor);
     }
@@ -375,7 +378,7 @@ __global__ void __launch_bounds__(256) slice_rows_kernel(
     // keeps the slices
     const size_t e = (size_t)r * Kp + q;
     if (ops.Gh)
-      rot_ops_store2(ops, e, s0, s1);
+      rot_ops_store2(ops, e, s0, s1, h0, h1);
     else
       *reinterpret_cast<float2*>(S + e) = make_float2(s0, s1);
   }
@@ -772,7 +775,7 @@ __global__ void finite_sum_kernel(const double* __restrict__ x, int n, double* _
 //   when Ql != nullptr), each row scaled by 2^e_r so its largest entry sits
 //   near 2^14 (qscale_r = 2^-e_r); with stage, the row is kept in shared
 //   memory between the two passes, else the second pass re-reads it.
-constexpr int kMprepThreads = 1024;
+constexpr int kMprepThreads = 512;  // two blocks per SM (60 registers per thread)
 constexpr int kMprepStageMax = 30720;  // patterns whose row of Q fits shared memory (120 KB)
 
 __global__ void __launch_bounds__(kMprepThreads) mprep_kernel(
@@ -979,9 +982,9 @@ __device__ __forceinline__ void insert_point(const InsertCtx& c, const RotMat& R
                                              float z, float val, float w) {
   const int side = c.side;
   if (c.interp == EMC_INTERP_NEAREST) {
-    const long ix = lroundf(voxel_coord(side, rotate_row(R, 0, x, y, z)));
-    const long iy = lroundf(voxel_coord(side, rotate_row(R, 1, x, y, z)));
-    const long iz = lroundf(voxel_coord(side, rotate_row(R, 2, x, y, z)));
+    const long ix = voxel_round(voxel_coord(side, rotate_row(R, 0, x, y, z)));
+    const long iy = voxel_round(voxel_coord(side, rotate_row(R, 1, x, y, z)));
+    const long iz = voxel_round(voxel_coord(side, rotate_row(R, 2, x, y, z)));
     if (ix < 0 || ix >= side || iy < 0 || iy >= side || iz < 0 || iz >= side) return;
     add_voxel(c, ((size_t)iz * side + iy) * side + ix, val, w);
   } else {

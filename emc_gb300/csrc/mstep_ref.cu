@@ -104,9 +104,9 @@ __global__ void insert_nearest_kernel(const float* __restrict__ slices,
   if (__ldg(mask + p) != 1 || !(s >= 0.0f)) return;
   const RotMat R = sR;
   const float x = __ldg(xc + p), y = __ldg(yc + p), z = __ldg(zc + p);
-  const long ix = lroundf(voxel_coord(side, rotate_row(R, 0, x, y, z)));
-  const long iy = lroundf(voxel_coord(side, rotate_row(R, 1, x, y, z)));
-  const long iz = lroundf(voxel_coord(side, rotate_row(R, 2, x, y, z)));
+  const long ix = voxel_round(voxel_coord(side, rotate_row(R, 0, x, y, z)));
+  const long iy = voxel_round(voxel_coord(side, rotate_row(R, 1, x, y, z)));
+  const long iz = voxel_round(voxel_coord(side, rotate_row(R, 2, x, y, z)));
   if (ix < 0 || ix >= side || iy < 0 || iy >= side || iz < 0 || iz >= side) return;
   const size_t v = ((size_t)iz * side + iy) * side + ix;
   atomicAdd(model + v, __fmul_rn(w, s));

@@ -177,9 +177,11 @@ __device__ __forceinline__ void rot_ops_store(const RotOps& o, size_t e, float s
   if (o.Hl) o.Hl[e] = __float2half_rn(h - __half2float(hh));
 }
 
-// The operands of two neighbouring pixels e, e + 1 (e even) as 4-byte stores.
-__device__ __forceinline__ void rot_ops_store2(const RotOps& o, size_t e, float s0, float s1) {
-  const float sv[2] = {s0, s1};
+// The operands of two neighbouring pixels e, e + 1 (e even) as 4-byte stores;
+// h0, h1 = 1 / (s + 0.02) where s > 0 (0 elsewhere), computed by the caller.
+__device__ __forceinline__ void rot_ops_store2(const RotOps& o, size_t e, float s0, float s1,
+                                               float h0, float h1) {
+  const float sv[2] = {s0, s1}, hv[2] = {h0, h1};
   if (o.logs) {
     __half2 hi, lo;
     __half* ph = reinterpret_cast<__half*>(&hi);
@@ -205,7 +207,7 @@ __device__ __forceinline__ void rot_ops_store2(const RotOps& o, size_t e, float 
     const bool m = s > 0.0f;
     const float ms = mp ? s * (1.0f / 256.0f) : 0.0f;
     if (ms > 60000.0f) atomicOr(o.flags, 4);
-    const float h = m ? 1.0f / (s + 0.02f) : 0.0f;
+    const float h = hv[u];
     const float g = m ? s * h : 0.0f;
     pmp[u] = __float2half_rn(mp ? 1.0f : 0.0f);
     pms[u] = __float2half_rn(ms);

@@ -17,9 +17,9 @@ namespace emc {
 // outside (emc_cuda.cu:132-134), everything outside gives -1.
 __device__ __forceinline__ float sample_nearest(const float* __restrict__ model, int side,
                                                 const RotMat& R, float x, float y, float z) {
-  const long ix = lroundf(voxel_coord(side, rotate_row(R, 0, x, y, z)));
-  const long iy = lroundf(voxel_coord(side, rotate_row(R, 1, x, y, z)));
-  const long iz = lroundf(voxel_coord(side, rotate_row(R, 2, x, y, z)));
+  const long ix = voxel_round(voxel_coord(side, rotate_row(R, 0, x, y, z)));
+  const long iy = voxel_round(voxel_coord(side, rotate_row(R, 1, x, y, z)));
+  const long iz = voxel_round(voxel_coord(side, rotate_row(R, 2, x, y, z)));
   if (ix > 0 && ix < side && iy > 0 && iy < side && iz > 0 && iz < side)
     return __ldg(model + ((size_t)iz * side + iy) * side + ix);
   return -1.0f;

@@ -881,9 +881,9 @@ __device__ __forceinline__ void tc_insert(const TcMstepArgs& a, const RotMat& R,
                                           float y, float z, float val, float w) {
   const int side = a.side;
   if (a.interp == EMC_INTERP_NEAREST) {
-    const long ix = lroundf(voxel_coord(side, rotate_row(R, 0, x, y, z)));
-    const long iy = lroundf(voxel_coord(side, rotate_row(R, 1, x, y, z)));
-    const long iz = lroundf(voxel_coord(side, rotate_row(R, 2, x, y, z)));
+    const long ix = voxel_round(voxel_coord(side, rotate_row(R, 0, x, y, z)));
+    const long iy = voxel_round(voxel_coord(side, rotate_row(R, 1, x, y, z)));
+    const long iz = voxel_round(voxel_coord(side, rotate_row(R, 2, x, y, z)));
     const bool in = on && ix >= 0 && ix < side && iy >= 0 && iy < side && iz >= 0 && iz < side;
     tc_insert_nearest(a, in, in ? ((long long)iz * side + iy) * side + ix : -1, val, w);
   } else {

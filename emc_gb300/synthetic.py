@@ -53,6 +53,9 @@ CONFIGS = {
     "large": Config("large", 256, 20000, 1.5, 56, 100000, 10000, (0.5, 1.5), 12, 12, 5),
     # the mid geometry with a fifth of the patterns: kernel profiles of a few GB
     "mid_small": Config("mid_small", 128, 3000, 1.5, 28, 4000, 5000, (0.5, 1.5), 6, 8, 1),
+    # the mid geometry and patterns with the 6,300 rotations of level 5: profiles of the
+    # per-row kernels (expand, mprep) on a few GB
+    "mid_r5": Config("mid_r5", 128, 3000, 1.5, 28, 20000, 5000, (0.5, 1.5), 6, 5, 1),
 }
 
 

@@ -48,7 +48,7 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--config", default="mid")
     ap.add_argument("--precision", choices=["auto", "mixed", "fp32"], default="auto")
-    ap.add_argument("--insert", choices=["atomic", "deterministic"], default="atomic")
+    ap.add_argument("--insert", choices=["atomic", "deterministic", "sorted"], default="atomic")
     ap.add_argument("--mstep-qlo", type=int, choices=[0, 1], default=0,
                     help="tensor M-step: responsibility x scaling as FP16 hi+lo (1) or hi (0)")
     ap.add_argument("--diff", choices=["poisson", "true_poisson"], default="poisson",
@@ -298,7 +298,8 @@ def run_ours(args):
     T = lambda a, dt=torch.float32: torch.as_tensor(np.ascontiguousarray(a), dtype=dt, device=dev)
     images, mask = T(prob.images), T(prob.mask, torch.int32)
     x, y, z, rot, w = T(prob.x), T(prob.y), T(prob.z), T(prob.quats), T(prob.weights)
-    insert = E.INSERT_DETERMINISTIC if args.insert == "deterministic" else E.INSERT_ATOMIC
+    insert = {"atomic": E.INSERT_ATOMIC, "deterministic": E.INSERT_DETERMINISTIC,
+              "sorted": E.INSERT_SORTED}[args.insert]
 
     def new_plan(prec):
         diff = E.DIFF_TRUE_POISSON if args.diff == "true_poisson" else E.DIFF_POISSON

@@ -23,7 +23,8 @@ import numpy as np
 
 from . import _lib
 from ._lib import (DIFF_ABSOLUTE, DIFF_POISSON, DIFF_RELATIVE, DIFF_TRUE_POISSON,  # noqa: F401
-                   INSERT_ATOMIC, INSERT_DETERMINISTIC, INTERP_NEAREST, INTERP_TRILINEAR,
+                   INSERT_ATOMIC, INSERT_DETERMINISTIC, INSERT_SORTED, INTERP_NEAREST,
+                   INTERP_TRILINEAR,
                    PREC_FP32, PREC_MIXED, EmcError, IterStats, PlanDesc)
 
 __all__ = [

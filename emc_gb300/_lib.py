@@ -26,7 +26,7 @@ ERRORS = {
 DIFF_ABSOLUTE, DIFF_POISSON, DIFF_RELATIVE, DIFF_TRUE_POISSON = 0, 1, 2, 3
 INTERP_NEAREST, INTERP_TRILINEAR = 0, 1
 PREC_FP32, PREC_MIXED = 0, 1
-INSERT_ATOMIC, INSERT_DETERMINISTIC = 0, 1
+INSERT_ATOMIC, INSERT_DETERMINISTIC, INSERT_SORTED = 0, 1, 2
 
 P = C.c_void_p
 I = C.c_int

@@ -2,7 +2,7 @@
 // reference's main.cpp:34-521 for one process on one GPU.  It uses only the
 // C ABI of libemc_gb300.so.
 //
-//   emc [config] [--dropin] [--precision fp32|mixed] [--deterministic]
+//   emc [config] [--dropin] [--precision fp32|mixed] [--deterministic | --sorted-insert]
 //       [--interp nearest|trilinear] [--out DIR] [--iterations N] [--graph]
 //       [--prune] [--no-autotune]
 //
@@ -131,6 +131,7 @@ Opts parse_args(int argc, char** argv) {
     };
     if (a == "--dropin") o.dropin = true;
     else if (a == "--deterministic") o.insert = EMC_INSERT_DETERMINISTIC;
+    else if (a == "--sorted-insert") o.insert = EMC_INSERT_SORTED;
     else if (a == "--precision") o.precision = next() == "mixed" ? EMC_PREC_MIXED : EMC_PREC_FP32;
     else if (a == "--interp") o.interp = next() == "trilinear" ? EMC_INTERP_TRILINEAR : EMC_INTERP_NEAREST;
     else if (a == "--out") o.out = next();

@@ -954,22 +954,19 @@ struct InsertCtx {
   unsigned long long* fix_m;
   unsigned long long* fix_w;
   float2* acc2;          // interleaved (model, weight) sums: one 8-byte atomic per point
-  const double* bounds;  // {model, weight} inserted-mass bounds (deterministic mode)
+  const float2* fix_scale;  // {model, weight} fixed-point scales (deterministic mode)
+  float* u;              // sorted mode: pair values [P_eff][ldu] instead of insertion
+  int ldu;
   int side;
   int interp;
   int deterministic;
 };
 
-// Fixed-point scale of the deterministic insertion: 2^61 / bound, so no
-// partial sum can leave the signed 64-bit range.
-__host__ __device__ inline double fixed_scale(double bound) {
-  return bound > 0.0 ? 2305843009213693952.0 / bound : 1.0;
-}
-
 __device__ __forceinline__ void add_voxel(const InsertCtx& c, size_t v, float val, float w) {
   if (c.deterministic) {
-    atomicAdd(c.fix_m + v, (unsigned long long)__double2ll_rn((double)val * fixed_scale(c.bounds[0])));
-    atomicAdd(c.fix_w + v, (unsigned long long)__double2ll_rn((double)w * fixed_scale(c.bounds[1])));
+    const float2 sc = __ldg(c.fix_scale);
+    atomicAdd(c.fix_m + v, (unsigned long long)fixed_from_float(__fmul_rn(val, sc.x)));
+    atomicAdd(c.fix_w + v, (unsigned long long)fixed_from_float(__fmul_rn(w, sc.y)));
   } else {
     atomicAdd(c.acc2 + v, make_float2(val, w));
   }
@@ -1084,6 +1081,16 @@ __global__ void __launch_bounds__(TPB, 1) mstep_fp32_kernel(MstepArgs a) {
     const int r = r0 + rl;
     if (r >= a.R) continue;
     const float t = __ldg(a.T + r);
+    if (a.ins.u) {  // sorted mode: the pair values, 0 where the rotation inserts nothing
+      const bool live = t > 1e-10f;
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        const int q = q0 + micro_idx(tx4, j);
+        if (q < a.P_eff)
+          a.ins.u[(size_t)q * a.ins.ldu + r] = live ? __fmul_rn(t, __fdiv_rn(acc[i][j], t)) : 0.0f;
+      }
+      continue;
+    }
     if (!(t > 1e-10f)) continue;
     const RotMat R = sR[rl];
 #pragma unroll
@@ -1099,10 +1106,11 @@ __global__ void __launch_bounds__(TPB, 1) mstep_fp32_kernel(MstepArgs a) {
 
 // ------------------------------------------------------- finishing -------
 // Upper bounds of the inserted model and weight mass (deterministic mode):
-// 1.25 * sum_r sum_i Q_ri K_i and 1.25 * P_eff * sum_r T_r, FP64, fixed order.
+// 1.25 * sum_r sum_i Q_ri K_i and 1.25 * P_eff * sum_r T_r, FP64, fixed order,
+// and the fixed-point scales they give.
 __global__ void insert_bounds_kernel(const double* __restrict__ row_mass,
                                      const double* __restrict__ row_bound, int R, int P_eff,
-                                     double* __restrict__ out) {
+                                     double* __restrict__ out, float2* __restrict__ scale) {
   __shared__ double sm[256], sw[256];
   double m = 0.0, w = 0.0;
   for (int r = threadIdx.x; r < R; r += blockDim.x) {
@@ -1122,6 +1130,7 @@ __global__ void insert_bounds_kernel(const double* __restrict__ row_mass,
   if (threadIdx.x == 0) {
     out[0] = 1.25 * sm[0] + 1e-30;
     out[1] = 1.25 * sw[0] * (double)P_eff + 1e-30;
+    *scale = make_float2(fix_scale_pow2(out[0]), fix_scale_pow2(out[1]));
   }
 }
 
@@ -1130,11 +1139,11 @@ __global__ void insert_bounds_kernel(const double* __restrict__ row_mass,
 // interleaved float accumulators.
 __global__ void finish_insert_kernel(const unsigned long long* __restrict__ fm,
                                      const unsigned long long* __restrict__ fw,
-                                     const double* __restrict__ bounds,
+                                     const float2* __restrict__ fix_scale,
                                      const float2* __restrict__ acc2, float* __restrict__ model,
                                      float* __restrict__ weight, long long n) {
-  const double inv_m = fm ? 1.0 / fixed_scale(bounds[0]) : 0.0;
-  const double inv_w = fm ? 1.0 / fixed_scale(bounds[1]) : 0.0;
+  const float2 sc = fm ? *fix_scale : make_float2(1.0f, 1.0f);
+  const double inv_m = 1.0 / (double)sc.x, inv_w = 1.0 / (double)sc.y;  // powers of two
   const long long stride = (long long)gridDim.x * blockDim.x;
   for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += stride) {
     float m, w;
@@ -1186,10 +1195,11 @@ __global__ void lse_from_global_kernel(const double* __restrict__ lse_in, int N,
 // exactly as finish_insert_kernel reads them.
 __global__ void sums_out_kernel(const unsigned long long* __restrict__ fm,
                                 const unsigned long long* __restrict__ fw,
-                                const double* __restrict__ bounds, const float2* __restrict__ acc2,
+                                const float2* __restrict__ fix_scale,
+                                const float2* __restrict__ acc2,
                                 float* __restrict__ msum, float* __restrict__ wsum, long long n) {
-  const double inv_m = fm ? 1.0 / fixed_scale(bounds[0]) : 0.0;
-  const double inv_w = fm ? 1.0 / fixed_scale(bounds[1]) : 0.0;
+  const float2 sc = fm ? *fix_scale : make_float2(1.0f, 1.0f);
+  const double inv_m = 1.0 / (double)sc.x, inv_w = 1.0 / (double)sc.y;  // powers of two
   const long long stride = (long long)gridDim.x * blockDim.x;
   for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += stride) {
     if (fm) {
@@ -1237,7 +1247,9 @@ extern "C" int emc_plan_create(emc_ctx* ctx, const emc_plan_desc* desc, emc_plan
               "plan_create: bad interp");
   EMC_REQUIRE(ctx, d.precision == EMC_PREC_FP32 || d.precision == EMC_PREC_MIXED,
               "plan_create: bad precision");
-  EMC_REQUIRE(ctx, d.insert_mode == EMC_INSERT_ATOMIC || d.insert_mode == EMC_INSERT_DETERMINISTIC,
+  EMC_REQUIRE(ctx,
+              d.insert_mode == EMC_INSERT_ATOMIC || d.insert_mode == EMC_INSERT_DETERMINISTIC ||
+                  d.insert_mode == EMC_INSERT_SORTED,
               "plan_create: bad insert mode");
   EMC_REQUIRE(ctx, d.blur_sigma >= 0.0f && std::isfinite(d.blur_sigma), "plan_create: bad blur");
   emc_plan* p = new emc_plan();
@@ -1293,7 +1305,7 @@ extern "C" int emc_plan_create(emc_ctx* ctx, const emc_plan_desc* desc, emc_plan
     rc = alloc_n(p, &p->fix_m, n3);
     if (!rc) rc = alloc_n(p, &p->fix_w, n3);
   }
-  if (!rc && d.insert_mode == EMC_INSERT_ATOMIC) rc = alloc_n(p, &p->acc2, n3);
+  if (!rc && d.insert_mode != EMC_INSERT_DETERMINISTIC) rc = alloc_n(p, &p->acc2, n3);
   if (rc) {
     emc_plan_destroy(p);
     return rc;
@@ -1306,6 +1318,7 @@ extern "C" int emc_plan_destroy(emc_plan* p) {
   if (!p) return EMC_OK;
   if (p->ctx) cudaStreamSynchronize(p->ctx->stream);
   prune_free(p);
+  sorted_free(p);
   if (p->graph_exec) cudaGraphExecDestroy(p->graph_exec);
   if (p->graph) cudaGraphDestroy(p->graph);
   for (auto& e : p->ev)
@@ -1455,6 +1468,11 @@ extern "C" int emc_plan_bind(emc_plan* p, const float* d_images, const int* d_ma
   // coherent order of its own rotations and a full scan
   if ((rc = prune_reset(p))) return rc;
   p->bound = true;
+  // sorted insertion: the voxel map of this binding's rotations and pixels
+  if ((rc = sorted_ensure(p))) {
+    p->bound = false;
+    return rc;
+  }
   return EMC_OK;
 }
 
@@ -1507,7 +1525,9 @@ static InsertCtx make_insert_ctx(emc_plan* p, float* model, float* weight) {
   c.fix_m = p->fix_m;
   c.fix_w = p->fix_w;
   c.acc2 = p->acc2;
-  c.bounds = p->red + kRedBoundM;
+  c.fix_scale = reinterpret_cast<const float2*>(p->red + kRedFixScale);
+  c.u = p->d.insert_mode == EMC_INSERT_SORTED ? p->ins_u : nullptr;
+  c.ldu = p->ins_ldu;
   c.side = p->d.side;
   c.interp = p->d.interp;
   c.deterministic = p->d.insert_mode == EMC_INSERT_DETERMINISTIC;
@@ -1614,19 +1634,21 @@ static int enqueue_mstep(emc_plan* p, float* d_model, float* d_weight) {
   if ((rc = mark_phase(p, 4))) return rc;
   const bool det = p->d.insert_mode == EMC_INSERT_DETERMINISTIC;
   if (det) {
-    insert_bounds_kernel<<<1, 256, 0, ctx->stream>>>(row_mass, row_bound, R, p->P_eff,
-                                                      p->red + kRedBoundM);
+    insert_bounds_kernel<<<1, 256, 0, ctx->stream>>>(
+        row_mass, row_bound, R, p->P_eff, p->red + kRedBoundM,
+        reinterpret_cast<float2*>(p->red + kRedFixScale));
     if ((rc = after_launch(ctx, "insert_bounds_kernel"))) return rc;
     EMC_CUDA(ctx, cudaMemsetAsync(p->fix_m, 0, sizeof(unsigned long long) * n3, ctx->stream));
     EMC_CUDA(ctx, cudaMemsetAsync(p->fix_w, 0, sizeof(unsigned long long) * n3, ctx->stream));
-  } else {
+  } else if (p->d.insert_mode == EMC_INSERT_ATOMIC) {
     EMC_CUDA(ctx, cudaMemsetAsync(p->acc2, 0, sizeof(float2) * n3, ctx->stream));
-  }
+  }  // sorted: the reduction writes every voxel of acc2
   InsertCtx ins = make_insert_ctx(p, d_model, d_weight);
   if (tcm)
     rc = tc_mstep(p, d_model, d_weight);
   else
     rc = plan_mstep_fp32(p, d_model, d_weight, ins);
+  if (!rc && p->d.insert_mode == EMC_INSERT_SORTED) rc = sorted_reduce(p);
   return rc;
 }
 
@@ -1639,7 +1661,8 @@ static int enqueue_finish(emc_plan* p, float* d_model, float* d_weight) {
   {
     const int nb = (int)std::min<long long>(ceil_div(n3, 256), (long long)ctx->sm_count * 8);
     finish_insert_kernel<<<nb, 256, 0, ctx->stream>>>(det ? p->fix_m : nullptr, p->fix_w,
-                                                       p->red + kRedBoundM, p->acc2, d_model,
+                                                       reinterpret_cast<const float2*>(p->red + kRedFixScale),
+                                                       p->acc2, d_model,
                                                        d_weight, n3);
     if ((rc = after_launch(ctx, "finish_insert_kernel"))) return rc;
   }
@@ -2032,7 +2055,8 @@ extern "C" int emc_rank_mstep(emc_plan* p, const double* d_lse, float* d_model_s
   const bool det = p->d.insert_mode == EMC_INSERT_DETERMINISTIC;
   const int nb = (int)std::min<long long>(ceil_div(n3, 256), (long long)ctx->sm_count * 8);
   sums_out_kernel<<<nb, 256, 0, ctx->stream>>>(det ? p->fix_m : nullptr, p->fix_w,
-                                                p->red + kRedBoundM, p->acc2, d_model_sum,
+                                                reinterpret_cast<const float2*>(p->red + kRedFixScale),
+                                                p->acc2, d_model_sum,
                                                 d_weight_sum, n3);
   return after_launch(ctx, "sums_out_kernel");
 }

@@ -112,6 +112,13 @@ struct emc_plan {
   unsigned debug_spin = 0;  // > 0: polls per tensor-pipeline wait (EMC_OPT_DEBUG_SPIN)
   int mstep_pair = 0;       // tensor M-step full scans on CTA pairs (EMC_OPT_MSTEP_PAIR)
 
+  // sorted-voxel insertion (EMC_INSERT_SORTED, sorted_insert.cu): the M-step
+  // stores each pair's value T_r x slice in ins_u [P_eff][ins_ldu] (rotation
+  // fastest) and a segmented reduction in voxel order adds them
+  float* ins_u = nullptr;
+  int ins_ldu = 0;
+  void* sorted = nullptr;
+
   std::vector<void*> allocs;
   size_t bytes = 0;
 };
@@ -126,10 +133,51 @@ enum RedSlot {
   kRedBoundM = 3,    // upper bound of inserted model mass
   kRedBoundW = 4,    // upper bound of inserted weight
   kRedMean = 5,      // {sum, count} of positive voxels (2 slots) + partials
+  kRedFixScale = 7,  // float2 {model, weight} fixed-point scales (deterministic mode)
   kRedSlots = 8,
 };
 
+// Deterministic insertion adds round(value * scale) into 64-bit integers.
+// The scale is the power of two 2^(61 - k) with bound <= 2^k (the bound is an
+// upper bound of the total inserted mass), so no partial sum leaves the signed
+// 64-bit range, value * scale is exact in FP32, and 1 / scale is exact too.
+__host__ __device__ inline float fix_scale_pow2(double bound) {
+  if (!(bound > 0.0)) return 1.0f;
+  int k;
+  frexp(bound, &k);  // bound = f 2^k, f in [0.5, 1)
+  const int e = 61 - k;
+  return ldexpf(1.0f, e < -126 ? -126 : (e > 126 ? 126 : e));
+}
+
+#ifdef __CUDACC__
+// x rounded to the nearest integer (ties to even) as a signed 64-bit value,
+// with FP32 and integer instructions only: below 2^23 the addition of 2^23
+// rounds the fraction away; from 2^23 on x is an integer, its mantissa shifted
+// by the exponent.  |x| >= 2^62 (never reached under fix_scale_pow2) saturates.
+__device__ __forceinline__ long long fixed_from_float(float x) {
+  const float a = fabsf(x);
+  long long m;
+  if (a < 8388608.0f) {
+    m = (long long)(__float_as_uint(__fadd_rn(a, 8388608.0f)) - 0x4B000000u);
+  } else if (a < 4611686018427387904.0f) {
+    const unsigned b = __float_as_uint(a);
+    m = (long long)((b & 0x7FFFFFu) | 0x800000u) << ((int)(b >> 23) - 150);
+  } else {
+    m = 0x4000000000000000LL;
+  }
+  return x < 0.0f ? -m : m;
+}
+#endif
+
 int plan_alloc(emc_plan* p, void** ptr, size_t bytes);
+
+// Sorted-voxel insertion (sorted_insert.cu).  sorted_ensure (re)builds the
+// voxel map when the plan's rotations or pixel coordinates differ from those
+// it was built from (a bind, a change of the rotation order); sorted_reduce
+// enqueues the per-iteration reduction of ins_u into acc2.
+int sorted_ensure(emc_plan* p);
+int sorted_reduce(emc_plan* p);
+void sorted_free(emc_plan* p);
 
 // Tensor-core path (tc_gemm.cu).
 int tc_bind(emc_plan* p);

@@ -539,9 +539,7 @@ int prune_iterate(emc_plan* p, float* model, float* weight, float sigma, emc_ite
 
 using namespace emc;
 
-extern "C" int emc_plan_set_pruning(emc_plan* p, int on, float min_mass, float dilate,
-                                    int full_every) {
-  if (!p) return EMC_ERR_INVALID;
+static int set_pruning(emc_plan* p, int on, float min_mass, float dilate, int full_every) {
   emc_ctx* ctx = p->ctx;
   if (!on) {
     if (p->prune) {
@@ -684,4 +682,13 @@ extern "C" int emc_plan_set_proposals(emc_plan* p, const float* d_quats, int n_m
       d_quats, n_modes, p->rot, R, N, ps->d_newpos, cos_half, n_rt, ps->d_core);
   if ((rc = after_launch(ctx, "proposal_core_kernel"))) return rc;
   return prune_finish(p, ps, order, probe_stride, true);  // order: position -> input pattern
+}
+
+extern "C" int emc_plan_set_pruning(emc_plan* p, int on, float min_mass, float dilate,
+                                    int full_every) {
+  if (!p) return EMC_ERR_INVALID;
+  int rc = set_pruning(p, on, min_mass, dilate, full_every);
+  // the rotation order may have changed: the sorted insertion's voxel map follows it
+  const int rc2 = sorted_ensure(p);
+  return rc ? rc : rc2;
 }

@@ -818,7 +818,9 @@ struct TcMstepArgs {
   unsigned long long* fix_m;
   unsigned long long* fix_w;
   float2* acc2;
-  const double* bounds;
+  const float2* fix_scale;  // {model, weight} fixed-point scales (deterministic mode)
+  float* u;                 // sorted mode: pair values [P_eff][ldu] instead of insertion
+  int ldu;
   int q_lo;  // 1: Q hi + lo, 0: Q hi only
   // pruned iteration: the pattern k-blocks of rotation tile rt are
   // kb_list[kb_off[rt] .. kb_off[rt+1]) (Q is zero elsewhere); nullptr: all
@@ -836,14 +838,11 @@ __device__ __forceinline__ int ms_kb(const TcMstepArgs& a, int rt, int j) {
   return a.kb_off ? a.kb_list[a.kb_off[rt] + j] : j;
 }
 
-__device__ __forceinline__ double tc_fixed_scale(double b) {
-  return b > 0.0 ? 2305843009213693952.0 / b : 1.0;
-}
-
 __device__ __forceinline__ void tc_add(const TcMstepArgs& a, size_t v, float val, float w) {
   if (a.deterministic) {
-    atomicAdd(a.fix_m + v, (unsigned long long)__double2ll_rn((double)val * tc_fixed_scale(a.bounds[0])));
-    atomicAdd(a.fix_w + v, (unsigned long long)__double2ll_rn((double)w * tc_fixed_scale(a.bounds[1])));
+    const float2 sc = __ldg(a.fix_scale);
+    atomicAdd(a.fix_m + v, (unsigned long long)fixed_from_float(__fmul_rn(val, sc.x)));
+    atomicAdd(a.fix_w + v, (unsigned long long)fixed_from_float(__fmul_rn(w, sc.y)));
   } else {
     atomicAdd(a.acc2 + v, make_float2(val, w));  // model and weight in one 8-byte atomic
   }
@@ -1053,8 +1052,12 @@ __global__ void __launch_bounds__(ms::THREADS, 1)
           if (q < a.P_eff) {  // uniform over the warp
             const float U = u[jj] * qs;
             const float slice = live ? U / Tr : 0.0f;
-            tc_insert(a, Rm, live, __ldg(a.cx + q), __ldg(a.cy + q), __ldg(a.cz + q), Tr * slice,
-                      Tr);
+            if (a.u) {  // sorted mode: a coalesced store per column (lanes: rotations)
+              if (rok) a.u[(size_t)q * a.ldu + r] = Tr * slice;
+            } else {
+              tc_insert(a, Rm, live, __ldg(a.cx + q), __ldg(a.cy + q), __ldg(a.cz + q),
+                        Tr * slice, Tr);
+            }
           }
         }
       }
@@ -1235,8 +1238,12 @@ __global__ void __launch_bounds__(ms::THREADS, 1)
           if (q < a.P_eff) {
             const float U = u[jj] * qs;
             const float slice = live ? U / Tr : 0.0f;
-            tc_insert(a, Rm, live, __ldg(a.cx + q), __ldg(a.cy + q), __ldg(a.cz + q), Tr * slice,
-                      Tr);
+            if (a.u) {  // sorted mode: a coalesced store per column (lanes: rotations)
+              if (rok) a.u[(size_t)q * a.ldu + r] = Tr * slice;
+            } else {
+              tc_insert(a, Rm, live, __ldg(a.cx + q), __ldg(a.cy + q), __ldg(a.cz + q),
+                        Tr * slice, Tr);
+            }
           }
         }
       }
@@ -1649,7 +1656,9 @@ int tc_mstep(emc_plan* p, float* model, float* weight) {
   a.aggregate = p->mstep_aggregate;
   a.kb_off = p->prune_kb_off;
   a.kb_list = p->prune_kb_list;
-  a.bounds = p->red + kRedBoundM;
+  a.fix_scale = reinterpret_cast<const float2*>(p->red + kRedFixScale);
+  a.u = p->d.insert_mode == EMC_INSERT_SORTED ? p->ins_u : nullptr;
+  a.ldu = p->ins_ldu;
   a.status = st->status;
   a.spin = p->debug_spin ? p->debug_spin : ptx::kSpinLimit;
   a.n_tiles = a.n_qt * a.n_rt;

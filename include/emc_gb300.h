@@ -60,6 +60,9 @@ extern "C" {
 /* model insertion of the fused iteration */
 #define EMC_INSERT_ATOMIC 0        /* float atomics (order-dependent rounding) */
 #define EMC_INSERT_DETERMINISTIC 1 /* order-independent: bit-identical reruns  */
+#define EMC_INSERT_SORTED 2        /* segmented reduction over voxel-sorted     \
+                                      pairs, fixed FP32 order: bit-identical    \
+                                      reruns (the pair map is built at bind)    */
 
 typedef struct emc_ctx emc_ctx;
 typedef struct emc_plan emc_plan;

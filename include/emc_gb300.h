@@ -315,7 +315,10 @@ size_t emc_plan_workspace_bytes(const emc_plan* plan);
  * use) and pre-processes the patterns (FP16 count operands, compaction to
  * the masked pixels).  images [N*s*s], mask [s*s], coords [s*s] x3,
  * rotations [4R], rotation weights [R].  May be called again (new pattern
- * data, same mask pixel count) without reallocating. */
+ * data, same mask pixel count) without reallocating.  With EMC_INSERT_SORTED
+ * it also builds the voxel-sorted pair map (synchronously; kept by a re-bind
+ * whose rotations and pixel coordinates are unchanged); EMC_ERR_UNSUPPORTED
+ * when a pair code (pixel, rotation[, corner]) does not fit 32 bits. */
 int emc_plan_bind(emc_plan* plan, const float* d_images, const int* d_mask, const float* d_x,
                   const float* d_y, const float* d_z, const float* d_rot,
                   const float* d_rot_weights);

@@ -457,6 +457,7 @@ class Plan:
     OPT_MSTEP_RASTER = 8
     OPT_DEBUG_SPIN = 9
     OPT_MSTEP_PAIR = 10
+    OPT_GLO_TAIL = 11
 
     def set_option(self, option: int, value: int):
         self.ctx._check(self._lib.emc_plan_set_option(self._h, option, value), "plan_set_option")

@@ -1938,6 +1938,11 @@ extern "C" int emc_plan_set_option(emc_plan* p, int option, int value) {
     p->counts_round = value;
     return EMC_OK;
   }
+  if (option == EMC_OPT_GLO_TAIL) {
+    EMC_REQUIRE(ctx, value >= 0 && value <= 1000000, "plan_set_option: G lo tail %d", value);
+    p->glo_tail_ppm = value;
+    return p->tc ? tc_glo_extent(p) : EMC_OK;
+  }
   if (option == EMC_OPT_MSTEP_QLO) {
     EMC_REQUIRE(ctx, value == 0 || value == 1, "plan_set_option: q_lo %d", value);
     p->mstep_q_lo = value;

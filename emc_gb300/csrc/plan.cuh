@@ -53,6 +53,11 @@ struct emc_plan {
   __half* K2hi = nullptr;    // fp16(k^2 * 2^-e)
   __half* K2lo = nullptr;    // k^2 * 2^-e - K2hi
   unsigned char* k2lo_any = nullptr;  // [Np/128][Kp/32] block has a nonzero K2lo
+  // [Np/128] the likelihood's G lo term runs on the k-blocks below glo_kb[pt]
+  // of pattern tile pt: the blocks after it hold at most glo_tail_ppm / 1e6 of
+  // every pattern's counts (EMC_OPT_GLO_TAIL; 0: G lo on every block)
+  int* glo_kb = nullptr;
+  int glo_tail_ppm = 1000;
   __half* KhT = nullptr;     // [Kp][Np] transposed counts for the M-step
 
   // rotation side, per iteration
@@ -187,6 +192,7 @@ void prune_free(emc_plan* p);
 int prune_reset(emc_plan* p);
 int tc_pattern_side(emc_plan* p, const int* d_perm, bool counts_done = false);
 int tc_ensure_qlo(emc_plan* p);
+int tc_glo_extent(emc_plan* p);  // glo_kb from the bound counts and glo_tail_ppm
 int pattern_side(emc_plan* p, const int* d_perm, bool with_tc);
 // Rotation-side FP16 operands of the tensor-core likelihood, written by the
 // expand kernel straight from each slice value s (no FP32 slice buffer):

@@ -129,6 +129,77 @@ __global__ void tc_k2lo_flags_kernel(const __half* __restrict__ K2l, int Kp,
   if (threadIdx.x == 0) flags[(size_t)pt * nkb + kb] = (unsigned char)any;
 }
 
+// glo_kb[pt] for pattern tile pt (one block of 256 threads): per pattern of
+// the tile, the sums of its counts over each 32-pixel block, their prefix
+// sums, and the last block b whose suffix (blocks b ..) still holds more than
+// eps of the pattern's total; glo_kb = 1 + the largest such b over the tile
+// (0 when every suffix is within eps).  Integer counts below 2^24 in total
+// sum exactly in FP32.  Shared memory: nkb floats.
+__global__ void __launch_bounds__(256) tc_glo_extent_kernel(const __half* __restrict__ Kh, int Kp,
+                                                            int nkb, int N, float eps,
+                                                            int* __restrict__ glo_kb) {
+  extern __shared__ float bsum[];
+  __shared__ float wpart[8];
+  __shared__ int wmax[8];
+  const int pt = blockIdx.x, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int per = (nkb + 255) / 256;  // consecutive blocks per thread in the scan
+  int last = -1;                      // this thread's largest b with suffix > eps
+  for (int row = 0; row < 128; ++row) {
+    const int n = pt * 128 + row;
+    if (n >= N) break;
+    const __half* k = Kh + (size_t)n * Kp;
+    for (int b = threadIdx.x; b < nkb; b += 256) {
+      const uint4* v = reinterpret_cast<const uint4*>(k + 32 * (size_t)b);
+      float s = 0.0f;
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const uint4 u = v[j];
+        const uint32_t w[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+        for (int h = 0; h < 4; ++h) {
+          const float2 f = __half22float2(*reinterpret_cast<const __half2*>(&w[h]));
+          s += f.x + f.y;
+        }
+      }
+      bsum[b] = s;
+    }
+    __syncthreads();
+    // this thread's chunk [b0, b1): its sum, then the block-wide prefix
+    const int b0 = min(threadIdx.x * per, nkb), b1 = min(b0 + per, nkb);
+    float c = 0.0f;
+    for (int b = b0; b < b1; ++b) c += bsum[b];
+    float inc = c;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const float t = __shfl_up_sync(0xffffffffu, inc, o);
+      if (lane >= o) inc += t;
+    }
+    if (lane == 31) wpart[warp] = inc;
+    __syncthreads();
+    float before = 0.0f, total = 0.0f;
+    for (int w = 0; w < 8; ++w) {
+      if (w < warp) before += wpart[w];
+      total += wpart[w];
+    }
+    float pre = before + inc - c;  // sum of the blocks before b0
+    const float lim = eps * total;
+    for (int b = b0; b < b1; ++b) {
+      if (total - pre > lim) last = max(last, b);  // suffix from b
+      pre += bsum[b];
+    }
+    __syncthreads();  // bsum and wpart are rewritten for the next row
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) last = max(last, __shfl_xor_sync(0xffffffffu, last, o));
+  if (lane == 0) wmax[warp] = last;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int m = -1;
+    for (int w = 0; w < 8; ++w) m = max(m, wmax[w]);
+    glo_kb[pt] = m + 1;
+  }
+}
+
 // [rows][cols] -> [cols][rows], FP16: 64 x 64 tiles, moved with 4-byte
 // (half2) loads and stores where two neighbouring elements are in range.
 __global__ void transpose_h_kernel(const __half* __restrict__ in, int rows, int cols,
@@ -220,6 +291,7 @@ struct TcEstepArgs {
   int gh_lo;                      // lo terms: bit 0 G, bit 1 H (3: both, 0: hi only)
   const int2* tiles;              // pruned iteration: (pattern tile, rotation tile) per CTA
   const unsigned char* k2lo_any;  // [n_pt][nkb]
+  const int* glo_kb;              // [n_pt] G lo runs on k-blocks below glo_kb[pt]
   const float* rot_cnt;
   const float* rot_A;
   const float* rotw;
@@ -371,7 +443,8 @@ __global__ void __launch_bounds__(es::THREADS, 1)
   ptx::tc_fence_after();
   const uint32_t tmem = *tmem_slot;
   const unsigned char* flags = a.k2lo_any + (size_t)pt * a.nkb;
-  const bool glo = (a.gh_lo & 1) != 0, hlo = (a.gh_lo & 2) != 0;
+  const bool hlo = (a.gh_lo & 2) != 0;
+  const int glo_end = (a.gh_lo & 1) ? a.glo_kb[pt] : 0;  // G lo on k-blocks below it
 
   if (warp == 0) {
     // ------------------------------------------------ TMA producer
@@ -383,6 +456,7 @@ __global__ void __launch_bounds__(es::THREADS, 1)
         const uint32_t ph = (kb / STAGES) & 1;
         if (!ptx::mbar_wait(&empty[s], ph ^ 1, a.status, 0, a.spin)) break;
         const bool lo = flags[kb] != 0;
+        const bool glo = kb < glo_end;
         const int ntiles = kSlots - (lo ? 0 : 1) - (glo ? 0 : 1) - (hlo ? 0 : 1);
         ptx::mbar_arrive_expect_tx(&full[s], ntiles * TILE_BYTES);
         unsigned char* st = smem + s * STAGE_BYTES;
@@ -407,6 +481,7 @@ __global__ void __launch_bounds__(es::THREADS, 1)
         if (!ptx::mbar_wait(&full[s], ph, a.status, 1, a.spin)) break;
         ptx::tc_fence_after();
         const bool lo = flags[kb] != 0;
+        const bool glo = kb < glo_end;
         const uint32_t base = ptx::smem_u32(smem + s * STAGE_BYTES);
 #pragma unroll
         for (int ks = 0; ks < BK / 16; ++ks) {
@@ -531,7 +606,9 @@ __global__ void __launch_bounds__(es::THREADS, 1)
   const int pt0 = 2 * ptp, pt1 = 2 * ptp + 1;
   const unsigned char* flags0 = a.k2lo_any + (size_t)pt0 * a.nkb;
   const unsigned char* flags1 = pt1 < a.n_pt ? a.k2lo_any + (size_t)pt1 * a.nkb : nullptr;
-  const bool glo = (a.gh_lo & 1) != 0;  // H lo (gh_lo bit 1) runs on single CTAs
+  // G lo on the k-blocks either pattern tile needs (H lo, gh_lo bit 1, runs on single CTAs)
+  const int glo_end =
+      (a.gh_lo & 1) ? max(a.glo_kb[pt0], pt1 < a.n_pt ? a.glo_kb[pt1] : 0) : 0;
 
   if (warp == 0) {
     // ------------------------------------------------ TMA producer (both CTAs)
@@ -544,6 +621,7 @@ __global__ void __launch_bounds__(es::THREADS, 1)
         const uint32_t ph = (kb / STAGES) & 1;
         if (!ptx::mbar_wait(&empty[s], ph ^ 1, a.status, 0, a.spin)) break;
         const bool lo = flags0[kb] != 0 || (flags1 && flags1[kb] != 0);
+        const bool glo = kb < glo_end;
         const uint32_t bytes = (lo ? 5 : 4) * es2::TILE + (glo ? es2::HALF : 0);
         if (rank == 0) ptx::mbar_arrive_expect_tx(&full[s], 2 * bytes);  // both CTAs' loads
         const uint32_t fb = ptx::mapa_shared(ptx::smem_u32(&full[s]), 0);
@@ -570,6 +648,7 @@ __global__ void __launch_bounds__(es::THREADS, 1)
         if (!ptx::mbar_wait(&full[s], ph, a.status, 1, a.spin)) break;
         ptx::tc_fence_after();
         const bool lo = flags0[kb] != 0 || (flags1 && flags1[kb] != 0);
+        const bool glo = kb < glo_end;
         const uint32_t base = ptx::smem_u32(smem + s * STAGE_BYTES);
 #pragma unroll
         for (int ks = 0; ks < BK / 16; ++ks) {
@@ -1312,6 +1391,7 @@ int tc_bind(emc_plan* p) {
       if (!rc) rc = plan_alloc(p, (void**)&p->K2hi, pk * 2);
       if (!rc) rc = plan_alloc(p, (void**)&p->K2lo, pk * 2);
       if (!rc) rc = plan_alloc(p, (void**)&p->k2lo_any, (size_t)(Np / 128) * (Kp / 32));
+      if (!rc) rc = plan_alloc(p, (void**)&p->glo_kb, sizeof(int) * (size_t)(Np / 128));
     }
     __half** rot_ops[6] = {&st->Gh, &st->Gl, &st->Mp, &st->MSh, &st->Hh, &st->Hl};
     for (int j = 0; j < (pois ? 2 : 6); ++j) {
@@ -1377,12 +1457,27 @@ int tc_pattern_side(emc_plan* p, const int* d_perm, bool counts_done) {
   if (!pois) tc_k2lo_flags_kernel<<<dim3(Kp / 32, Np / 128), 256, 0, ctx->stream>>>(p->K2lo, Kp, p->k2lo_any,
                                                                          Kp / 32);
   if ((rc = after_launch(ctx, "tc_k2lo_flags_kernel"))) return rc;
+  if (!pois && (rc = tc_glo_extent(p))) return rc;
   transpose_h_kernel<<<dim3(ceil_div(Kp, 64), ceil_div(Np, 64)), dim3(32, 8), 0, ctx->stream>>>(
       p->Kh, Np, Kp, p->KhT);
   return after_launch(ctx, "transpose_h_kernel");
 }
 
 int* tc_status(emc_plan* p) { return p->tc ? state(p)->status : nullptr; }
+
+int tc_glo_extent(emc_plan* p) {
+  if (!p->glo_kb) return EMC_OK;  // true Poisson: no G operand
+  emc_ctx* ctx = p->ctx;
+  const int nkb = p->Kp / es::BK, n_pt = p->Np / es::BM;
+  const size_t smem = sizeof(float) * (size_t)nkb;
+  if (smem > 48 * 1024) {
+    EMC_CUDA(ctx, cudaFuncSetAttribute(tc_glo_extent_kernel,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  }
+  tc_glo_extent_kernel<<<n_pt, 256, smem, ctx->stream>>>(
+      p->Kh, p->Kp, nkb, p->d.n_images, (float)p->glo_tail_ppm * 1e-6f, p->glo_kb);
+  return after_launch(ctx, "tc_glo_extent_kernel");
+}
 
 // The FP16 lo half of the M-step operand and its tensor map, allocated the
 // first time an M-step that uses it is requested (it is never read otherwise).
@@ -1448,6 +1543,7 @@ static int estep_launch(emc_plan* p, int raster, int first, int count, bool full
   a.gh_lo = p->estep_gh_lo >= 0 ? p->estep_gh_lo : (p->d.known_intensity ? 3 : 1);
   a.tiles = full ? nullptr : p->prune_tiles;
   a.k2lo_any = p->k2lo_any;
+  a.glo_kb = p->glo_kb;
   a.k2_inv = 1.0f / p->k2_scale;
   a.rot_cnt = p->rot_cnt;
   a.rot_A = p->rot_A;

@@ -493,6 +493,14 @@ int emc_batch_destroy(emc_batch* batch);
  * where a cluster launch is refused the plan falls back to single CTAs.
  * Results do not depend on it (bit for bit with deterministic insertion). */
 #define EMC_OPT_MSTEP_PAIR 10
+/* EMC_OPT_GLO_TAIL: the likelihood's G lo term (the FP16 lo half of
+ * G = s/(s+c) in B = K.G^T) is applied per 128-pattern tile up to the last
+ * 32-pixel block after which at most value / 1e6 of each pattern's counts
+ * remain (pixels are ordered by detector radius, so the dropped blocks are
+ * the dim outer ones): the term dropped there is below 2^-12 x value / 1e6
+ * of B.  Default 1000 (0.1 %); 0 applies it on every block.  Recomputed at
+ * once when the plan is bound. */
+#define EMC_OPT_GLO_TAIL 11
 int emc_plan_set_option(emc_plan* plan, int option, int value);
 /* Tile-order autotuner of the tensor-core likelihood kernel: expands d_model
  * (sigma as in emc_iterate), times the kernel for each candidate

@@ -46,20 +46,23 @@ def oracle_run(prob):
     return models, lls
 
 
-# mixed: the defaults (G hi + lo, H hi, Q hi); mixed-hilo: every factor hi + lo;
-# mixed-hi: every factor hi only (close to the log-likelihood target: the G lo
-# term matters, the H and Q lo terms do not)
-@pytest.mark.parametrize("precision,q_lo,gh_lo",
-                         [(E.PREC_FP32, 1, -1), (E.PREC_MIXED, 0, -1), (E.PREC_MIXED, 1, 3),
-                          (E.PREC_MIXED, 0, 0)],
-                         ids=["fp32", "mixed", "mixed-hilo", "mixed-hi"])
-def test_mid_geometry_accuracy(ctx, cuda, prob, oracle_run, precision, q_lo, gh_lo):
+# mixed: the defaults (G hi + lo up to the pattern tile's 0.1 % count tail,
+# H hi, Q hi); mixed-glo-all: G lo on every pixel block; mixed-hilo: every
+# factor hi + lo; mixed-hi: every factor hi only (close to the log-likelihood
+# target: the G lo term matters, the H and Q lo terms do not)
+@pytest.mark.parametrize("precision,q_lo,gh_lo,tail",
+                         [(E.PREC_FP32, 1, -1, 1000), (E.PREC_MIXED, 0, -1, 1000),
+                          (E.PREC_MIXED, 0, -1, 0), (E.PREC_MIXED, 1, 3, 0),
+                          (E.PREC_MIXED, 0, 0, 1000)],
+                         ids=["fp32", "mixed", "mixed-glo-all", "mixed-hilo", "mixed-hi"])
+def test_mid_geometry_accuracy(ctx, cuda, prob, oracle_run, precision, q_lo, gh_lo, tail):
     want_models, want_lls = oracle_run
     s, R, N = prob.cfg.side, prob.quats.shape[0], prob.images.shape[0]
     T = lambda a, dt=torch.float32: torch.as_tensor(np.ascontiguousarray(a), dtype=dt, device=cuda)
     plan = E.Plan(ctx, s, N, R, precision=precision)
     plan.set_option(E.Plan.OPT_MSTEP_QLO, q_lo)
     plan.set_option(E.Plan.OPT_ESTEP_GHLO, gh_lo)
+    plan.set_option(E.Plan.OPT_GLO_TAIL, tail)
     plan.bind(T(prob.images), T(prob.mask, torch.int32), T(prob.x), T(prob.y), T(prob.z),
               T(prob.quats), T(prob.weights))
     m = T(prob.init_model)
@@ -70,7 +73,8 @@ def test_mid_geometry_accuracy(ctx, cuda, prob, oracle_run, precision, q_lo, gh_
         want = want_models[it]
         rel = np.linalg.norm(got - want) / np.linalg.norm(want)
         ll_rel = abs(st.total_loglik - want_lls[it]) / abs(want_lls[it])
-        print(f"precision {precision} q_lo {q_lo} gh_lo {gh_lo} iteration {it}: model rel L2 {rel:.3e}, LL rel {ll_rel:.3e}")
+        print(f"precision {precision} q_lo {q_lo} gh_lo {gh_lo} tail {tail} iteration {it}: "
+              f"model rel L2 {rel:.3e}, LL rel {ll_rel:.3e}")
         assert rel < 1e-3
         assert ll_rel < 1e-4
     plan.close()

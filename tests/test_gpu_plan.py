@@ -74,6 +74,8 @@ MIXED_CASES = [
     # every factor hi + lo
     (dict(interp=E.INTERP_NEAREST, options={E.Plan.OPT_ESTEP_GHLO: 3, E.Plan.OPT_MSTEP_QLO: 1}),
      True),
+    # G lo on every pixel block (no count tail dropped)
+    (dict(interp=E.INTERP_NEAREST, options={E.Plan.OPT_GLO_TAIL: 0}), True),
 ]
 # tolerances: (log-likelihood rel, scaling rel, model rel L2, respons abs)
 TOL = {E.PREC_FP32: (1e-5, 1e-5, 1e-4, 1e-4), E.PREC_MIXED: (2e-5, 5e-4, 5e-4, 1e-3)}
@@ -130,7 +132,7 @@ def check_against_oracle(ctx, cuda, prob, kw, wellcond, precision):
 
 def case_id(c):
     names = {E.Plan.OPT_MSTEP_AGGREGATE: "aggregate", E.Plan.OPT_ESTEP_GHLO: "ghlo",
-             E.Plan.OPT_MSTEP_QLO: "qlo"}
+             E.Plan.OPT_MSTEP_QLO: "qlo", E.Plan.OPT_GLO_TAIL: "glotail"}
     return "-".join(f"{a}{b}" if a != "options" else
                     "-".join(f"{names[o]}{v}" for o, v in b.items()) for a, b in c[0].items())
 
@@ -168,6 +170,24 @@ def test_mixed_rejects_non_integer_counts(ctx, cuda, prob):
     p.images = prob.images + 0.5
     with pytest.raises(E.EmcError, match="UNSUPPORTED"):
         run_plan(ctx, p, cuda, precision=E.PREC_MIXED)
+
+
+@pytest.mark.parametrize("pair", [1, 0], ids=["pairs", "single"])
+def test_glo_tail_bounds(ctx, cuda, prob, pair):
+    """EMC_OPT_GLO_TAIL 1e6 (every block in the tail) drops the G lo term
+    everywhere: bit-identical to gh_lo = 0.  0 keeps it on every block that
+    holds a count; the default lies between and within the oracle bounds."""
+    kw = dict(precision=E.PREC_MIXED, insert_mode=E.INSERT_DETERMINISTIC)
+    base = {E.Plan.OPT_ESTEP_PAIR: pair}
+    none = run_plan(ctx, prob, cuda, options={**base, E.Plan.OPT_GLO_TAIL: 1000000}, **kw)
+    off = run_plan(ctx, prob, cuda, options={**base, E.Plan.OPT_ESTEP_GHLO: 0}, **kw)
+    assert np.array_equal(none["model"], off["model"])
+    assert none["stats"].total_loglik == off["stats"].total_loglik
+    every = run_plan(ctx, prob, cuda, options={**base, E.Plan.OPT_GLO_TAIL: 0}, **kw)
+    dflt = run_plan(ctx, prob, cuda, options=base, **kw)
+    ll_e, ll_d = every["stats"].total_loglik, dflt["stats"].total_loglik
+    assert abs(ll_d - ll_e) <= 1e-5 * abs(ll_e)
+    assert rel_l2(dflt["model"], every["model"]) < 1e-4
 
 
 def test_deterministic_insert_is_bit_identical(ctx, cuda, prob):

@@ -129,75 +129,55 @@ __global__ void tc_k2lo_flags_kernel(const __half* __restrict__ K2l, int Kp,
   if (threadIdx.x == 0) flags[(size_t)pt * nkb + kb] = (unsigned char)any;
 }
 
-// glo_kb[pt] for pattern tile pt (one block of 256 threads): per pattern of
-// the tile, the sums of its counts over each 32-pixel block, their prefix
-// sums, and the last block b whose suffix (blocks b ..) still holds more than
-// eps of the pattern's total; glo_kb = 1 + the largest such b over the tile
-// (0 when every suffix is within eps).  Integer counts below 2^24 in total
-// sum exactly in FP32.  Shared memory: nkb floats.
+// The sum of one 32-pixel block of an FP16 count row (64 bytes, 16-byte aligned).
+__device__ __forceinline__ float count_block_sum(const __half* k) {
+  const uint4* v = reinterpret_cast<const uint4*>(k);
+  float s = 0.0f;
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const uint4 u = v[j];
+    const uint32_t w[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+    for (int h = 0; h < 4; ++h) {
+      const float2 f = __half22float2(*reinterpret_cast<const __half2*>(&w[h]));
+      s += f.x + f.y;
+    }
+  }
+  return s;
+}
+
+// One warp per pattern row n: the last 32-pixel block b whose suffix (blocks
+// b ..) still holds more than eps of the row's counts; glo_kb[n / 128] (zeroed
+// before) becomes the largest b + 1 over the tile's rows.  Lane l takes a
+// contiguous run of blocks: run sums, a warp prefix scan, then a second walk
+// over its run.  Integer counts below 2^24 in total sum exactly in FP32.
 __global__ void __launch_bounds__(256) tc_glo_extent_kernel(const __half* __restrict__ Kh, int Kp,
                                                             int nkb, int N, float eps,
                                                             int* __restrict__ glo_kb) {
-  extern __shared__ float bsum[];
-  __shared__ float wpart[8];
-  __shared__ int wmax[8];
-  const int pt = blockIdx.x, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int per = (nkb + 255) / 256;  // consecutive blocks per thread in the scan
-  int last = -1;                      // this thread's largest b with suffix > eps
-  for (int row = 0; row < 128; ++row) {
-    const int n = pt * 128 + row;
-    if (n >= N) break;
-    const __half* k = Kh + (size_t)n * Kp;
-    for (int b = threadIdx.x; b < nkb; b += 256) {
-      const uint4* v = reinterpret_cast<const uint4*>(k + 32 * (size_t)b);
-      float s = 0.0f;
+  const int n = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+  if (n >= N) return;  // whole warps
+  const __half* k = Kh + (size_t)n * Kp;
+  const int per = (nkb + 31) / 32;
+  const int b0 = min(lane * per, nkb), b1 = min(b0 + per, nkb);
+  float c = 0.0f;
+  for (int b = b0; b < b1; ++b) c += count_block_sum(k + 32 * (size_t)b);
+  float inc = c;
 #pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        const uint4 u = v[j];
-        const uint32_t w[4] = {u.x, u.y, u.z, u.w};
-#pragma unroll
-        for (int h = 0; h < 4; ++h) {
-          const float2 f = __half22float2(*reinterpret_cast<const __half2*>(&w[h]));
-          s += f.x + f.y;
-        }
-      }
-      bsum[b] = s;
-    }
-    __syncthreads();
-    // this thread's chunk [b0, b1): its sum, then the block-wide prefix
-    const int b0 = min(threadIdx.x * per, nkb), b1 = min(b0 + per, nkb);
-    float c = 0.0f;
-    for (int b = b0; b < b1; ++b) c += bsum[b];
-    float inc = c;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const float t = __shfl_up_sync(0xffffffffu, inc, o);
-      if (lane >= o) inc += t;
-    }
-    if (lane == 31) wpart[warp] = inc;
-    __syncthreads();
-    float before = 0.0f, total = 0.0f;
-    for (int w = 0; w < 8; ++w) {
-      if (w < warp) before += wpart[w];
-      total += wpart[w];
-    }
-    float pre = before + inc - c;  // sum of the blocks before b0
-    const float lim = eps * total;
-    for (int b = b0; b < b1; ++b) {
-      if (total - pre > lim) last = max(last, b);  // suffix from b
-      pre += bsum[b];
-    }
-    __syncthreads();  // bsum and wpart are rewritten for the next row
+  for (int o = 1; o < 32; o <<= 1) {
+    const float t = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += t;
+  }
+  const float total = __shfl_sync(0xffffffffu, inc, 31);
+  const float lim = eps * total;
+  float pre = inc - c;  // the counts of the blocks before b0
+  int last = -1;
+  for (int b = b0; b < b1; ++b) {
+    if (total - pre > lim) last = b;  // the suffix from b
+    pre += count_block_sum(k + 32 * (size_t)b);
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) last = max(last, __shfl_xor_sync(0xffffffffu, last, o));
-  if (lane == 0) wmax[warp] = last;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    int m = -1;
-    for (int w = 0; w < 8; ++w) m = max(m, wmax[w]);
-    glo_kb[pt] = m + 1;
-  }
+  if (lane == 0 && last >= 0) atomicMax(glo_kb + n / 128, last + 1);
 }
 
 // [rows][cols] -> [cols][rows], FP16: 64 x 64 tiles, moved with 4-byte
@@ -1469,12 +1449,8 @@ int tc_glo_extent(emc_plan* p) {
   if (!p->glo_kb) return EMC_OK;  // true Poisson: no G operand
   emc_ctx* ctx = p->ctx;
   const int nkb = p->Kp / es::BK, n_pt = p->Np / es::BM;
-  const size_t smem = sizeof(float) * (size_t)nkb;
-  if (smem > 48 * 1024) {
-    EMC_CUDA(ctx, cudaFuncSetAttribute(tc_glo_extent_kernel,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  }
-  tc_glo_extent_kernel<<<n_pt, 256, smem, ctx->stream>>>(
+  EMC_CUDA(ctx, cudaMemsetAsync(p->glo_kb, 0, sizeof(int) * (size_t)n_pt, ctx->stream));
+  tc_glo_extent_kernel<<<ceil_div(p->d.n_images, 8), 256, 0, ctx->stream>>>(
       p->Kh, p->Kp, nkb, p->d.n_images, (float)p->glo_tail_ppm * 1e-6f, p->glo_kb);
   return after_launch(ctx, "tc_glo_extent_kernel");
 }

@@ -330,9 +330,15 @@ __device__ __forceinline__ float plan_sample<EMC_INTERP_TRILINEAR>(const float* 
   return wsum > 1e-6f ? acc / wsum : -1.0f;
 }
 
-// One block per rotation: the compacted slice row S[r][0..Kp) and the
-// per-rotation sums: count_r (s > 0), A_r = sum s^2/(s+c) and the floored
-// slice sum of the true-Poisson likelihood.
+// The compacted slice rows S[r][0..Kp) (or their FP16 operands) of
+// kSliceRows rotations per block and the per-rotation sums: count_r (s > 0),
+// A_r = sum s^2/(s+c) and the floored slice sum of the true-Poisson
+// likelihood.
+// rotations per expand block: four with nearest sampling, two with the
+// eight-voxel trilinear gather (registers)
+template <int INTERP>
+__host__ __device__ constexpr int slice_rows_per_block() { return INTERP == EMC_INTERP_NEAREST ? 4 : 2; }
+
 template <int INTERP>
 __global__ void __launch_bounds__(256) slice_rows_kernel(
     const float* __restrict__ model, int side, const float* __restrict__ rot,
@@ -340,65 +346,88 @@ __global__ void __launch_bounds__(256) slice_rows_kernel(
     const float* __restrict__ cz, int R, int Kp, float* __restrict__ S,
     float* __restrict__ rot_cnt, float* __restrict__ rot_A, float* __restrict__ rot_ssum,
     RotOps ops) {
-  const int r = blockIdx.x;
-  __shared__ RotMat sR;
-  if (threadIdx.x == 0) sR = quat_to_matrix(rot + 4 * (size_t)r);
+  // kSliceRows rotations per block: each thread loads the coordinates of four
+  // neighbouring compacted pixels once (16-byte loads) and samples them for
+  // every rotation of the block, so coordinate traffic is shared and the
+  // model gathers of several rotations are in flight together; the operands
+  // go out as 8-byte stores (Kp is a multiple of 128)
+  constexpr int kSliceRows = slice_rows_per_block<INTERP>();
+  const int r0 = blockIdx.x * kSliceRows;
+  const int gl_end = ops.gl_end ? 32 * __ldg(ops.gl_end) : Kp;  // G lo pixels
+  const int nr = min(kSliceRows, R - r0);
+  __shared__ RotMat sR[kSliceRows];
+  if (threadIdx.x < nr) sR[threadIdx.x] = quat_to_matrix(rot + 4 * (size_t)(r0 + threadIdx.x));
   __syncthreads();
-  const RotMat Rm = sR;
   // per-thread FP32 partials (FP64 arithmetic is scarce on this GPU), block sums in FP64
-  float cnt = 0.0f, A = 0.0f, ss = 0.0f;
-  // two neighbouring pixels per thread and pass (Kp is a multiple of 128):
-  // their coordinates in 8-byte loads and the tensor path's six operand
-  // planes in 4-byte stores
-  for (int q = 2 * threadIdx.x; q < Kp; q += 2 * blockDim.x) {
-    const int2 pp = __ldg(reinterpret_cast<const int2*>(pix + q));
-    const float2 X = __ldg(reinterpret_cast<const float2*>(cx + q));
-    const float2 Y = __ldg(reinterpret_cast<const float2*>(cy + q));
-    const float2 Z = __ldg(reinterpret_cast<const float2*>(cz + q));
-    const float s0 = pp.x >= 0 ? plan_sample<INTERP>(model, side, Rm, X.x, Y.x, Z.x) : 0.0f;
-    const float s1 = pp.y >= 0 ? plan_sample<INTERP>(model, side, Rm, X.y, Y.y, Z.y) : 0.0f;
-    // one division per pixel: h = 1 / (s + c) serves A = s^2 h and the operands
-    const float h0 = s0 > 0.0f ? 1.0f / (s0 + kPoisC) : 0.0f;
-    const float h1 = s1 > 0.0f ? 1.0f / (s1 + kPoisC) : 0.0f;
-    if (pp.x >= 0) {
-      if (s0 > 0.0f) {
-        cnt += 1.0f;
-        A += s0 * s0 * h0;
+  float cnt[kSliceRows], A[kSliceRows], ss[kSliceRows];
+#pragma unroll
+  for (int k = 0; k < kSliceRows; ++k) cnt[k] = A[k] = ss[k] = 0.0f;
+  for (int q = 4 * threadIdx.x; q < Kp; q += 4 * blockDim.x) {
+    const int4 pp = __ldg(reinterpret_cast<const int4*>(pix + q));
+    const float4 X = __ldg(reinterpret_cast<const float4*>(cx + q));
+    const float4 Y = __ldg(reinterpret_cast<const float4*>(cy + q));
+    const float4 Z = __ldg(reinterpret_cast<const float4*>(cz + q));
+    const int pv[4] = {pp.x, pp.y, pp.z, pp.w};
+    const float xv[4] = {X.x, X.y, X.z, X.w}, yv[4] = {Y.x, Y.y, Y.z, Y.w},
+                zv[4] = {Z.x, Z.y, Z.z, Z.w};
+#pragma unroll
+    for (int k = 0; k < kSliceRows; ++k) {
+      if (k >= nr) break;  // uniform over the block
+      const RotMat Rm = sR[k];
+      float sv[4], hv[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+        sv[u] = pv[u] >= 0 ? plan_sample<INTERP>(model, side, Rm, xv[u], yv[u], zv[u]) : 0.0f;
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        // one division per pixel: h = 1 / (s + c) serves A = s^2 h and the operands
+        hv[u] = sv[u] > 0.0f ? 1.0f / (sv[u] + kPoisC) : 0.0f;
+        if (pv[u] >= 0) {
+          if (sv[u] > 0.0f) {
+            cnt[k] += 1.0f;
+            A[k] += sv[u] * sv[u] * hv[u];
+          }
+          ss[k] += fmaxf(sv[u], kSliceFloor);
+        }
       }
-      ss += fmaxf(s0, kSliceFloor);
+      // the tensor path takes its FP16 operands straight from s; the FP32
+      // path keeps the slices
+      const size_t e = (size_t)(r0 + k) * Kp + q;
+      if (ops.Gh)
+        rot_ops_store4(ops, e, sv, hv, q < gl_end);
+      else
+        *reinterpret_cast<float4*>(S + e) = make_float4(sv[0], sv[1], sv[2], sv[3]);
     }
-    if (pp.y >= 0) {
-      if (s1 > 0.0f) {
-        cnt += 1.0f;
-        A += s1 * s1 * h1;
-      }
-      ss += fmaxf(s1, kSliceFloor);
-    }
-    // the tensor path takes its FP16 operands straight from s; the FP32 path
-    // keeps the slices
-    const size_t e = (size_t)r * Kp + q;
-    if (ops.Gh)
-      rot_ops_store2(ops, e, s0, s1, h0, h1);
-    else
-      *reinterpret_cast<float2*>(S + e) = make_float2(s0, s1);
   }
-  __shared__ double sh[3][256];
-  sh[0][threadIdx.x] = (double)cnt;
-  sh[1][threadIdx.x] = (double)A;
-  sh[2][threadIdx.x] = (double)ss;
+  // per row: FP32 warp sums, then FP64 over the warps
+  __shared__ double wsum[3][kSliceRows][8];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < kSliceRows; ++k) {
+    float a = cnt[k], b = A[k], c = ss[k];
+    for (int o = 16; o > 0; o >>= 1) {
+      a += __shfl_down_sync(0xffffffffu, a, o);
+      b += __shfl_down_sync(0xffffffffu, b, o);
+      c += __shfl_down_sync(0xffffffffu, c, o);
+    }
+    if (lane == 0) {
+      wsum[0][k][warp] = (double)a;
+      wsum[1][k][warp] = (double)b;
+      wsum[2][k][warp] = (double)c;
+    }
+  }
   __syncthreads();
-  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-    if (threadIdx.x < o) {
-      sh[0][threadIdx.x] += sh[0][threadIdx.x + o];
-      sh[1][threadIdx.x] += sh[1][threadIdx.x + o];
-      sh[2][threadIdx.x] += sh[2][threadIdx.x + o];
+  if (threadIdx.x < nr) {
+    const int k = threadIdx.x;
+    double a = 0.0, b = 0.0, c = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+      a += wsum[0][k][w];
+      b += wsum[1][k][w];
+      c += wsum[2][k][w];
     }
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) {
-    rot_cnt[r] = (float)sh[0][0];
-    rot_A[r] = (float)sh[1][0];
-    rot_ssum[r] = (float)sh[2][0];
+    rot_cnt[r0 + k] = (float)a;
+    rot_A[r0 + k] = (float)b;
+    rot_ssum[r0 + k] = (float)c;
   }
 }
 
@@ -778,7 +807,7 @@ __global__ void finite_sum_kernel(const double* __restrict__ x, int n, double* _
 constexpr int kMprepThreads = 512;  // two blocks per SM (60 registers per thread)
 constexpr int kMprepStageMax = 30720;  // patterns whose row of Q fits shared memory (120 KB)
 
-__global__ void __launch_bounds__(kMprepThreads) mprep_kernel(
+__global__ void __launch_bounds__(kMprepThreads, 2) mprep_kernel(
     float* __restrict__ L, const float* __restrict__ PHI, const float2* __restrict__ lse2,
     const float* __restrict__ Ksum, const float* __restrict__ cnorm, int R, int N,
     float* __restrict__ Q, __half* __restrict__ Qh, __half* __restrict__ Ql,
@@ -791,17 +820,26 @@ __global__ void __launch_bounds__(kMprepThreads) mprep_kernel(
   // (P = 0), 1 evaluated, 2 evaluated margin tile (its mass is summed)
   const unsigned char* ts = tstate ? tstate + (r >> 7) : nullptr;
   float t = 0.0f, b = 0.0f, qmax = 0.0f, mg = 0.0f;
+  const bool fast = Qh != nullptr && Ql == nullptr;  // M-step operand FP16 hi only
   // one element: P = exp(L - lse) (0 outside the evaluated tiles), q = P / phi
   // (x c_i for the FP16 operand); returns q and stores P
   auto elem = [&](int i, int st, float l, float f, float2 li, float ks, float cn) -> float {
     float P = 0.0f;
     if (st) {
-      if (isfinite(li.x) && l > -INFINITY) P = expf((l - li.x) - li.y);
+      // an M-step operand of FP16 hi only takes P through an 11-bit rounding:
+      // the hardware exponential (2^-21 relative) serves it; Q hi + lo and the
+      // FP32 path keep expf
+      if (isfinite(li.x) && l > -INFINITY) {
+        const float x = (l - li.x) - li.y;
+        P = fast ? __expf(x) : expf(x);
+      }
       if (st == 2) mg += P;
     } else {
       f = 0.0f;
     }
-    float q = f > 0.0f ? __fdiv_rn(P, f) : 0.0f;
+    // q = P / phi correctly rounded, except for an FP16 hi-only operand, which
+    // a 2-ulp quotient changes at most in rare ties of its rounding
+    float q = f > 0.0f ? (fast ? __fdividef(P, f) : __fdiv_rn(P, f)) : 0.0f;
     t += P;
     b = __fmaf_rn(q, ks, b);
     if (Qh) q = __fmul_rn(q, cn);
@@ -818,11 +856,12 @@ __global__ void __launch_bounds__(kMprepThreads) mprep_kernel(
     const float4* S4 = reinterpret_cast<const float4*>(lse2);
     const float4* K4 = reinterpret_cast<const float4*>(Ksum);
     const float4* C4 = reinterpret_cast<const float4*>(cnorm);
-    for (int j = threadIdx.x; j < N / 4; j += blockDim.x) {
+    // two 4-tuples per thread and pass (j and j + blockDim, in that order, as
+    // one tuple per pass would take them): both tuples' row loads are in
+    // flight together
+    const int n4 = N / 4, bd = (int)blockDim.x;
+    auto tuple = [&](int j, int st, const float4& l, const float4& f) {
       const int i = 4 * j;
-      const int st = ts ? ts[(size_t)(i >> 7) * n_rt] : 1;
-      const float4 l = L4[j];
-      const float4 f = st ? F4[j] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
       const float4 s01 = S4[2 * j], s23 = S4[2 * j + 1];
       const float4 ks = __ldg(K4 + j), cn = __ldg(C4 + j);
       float4 P;
@@ -831,6 +870,19 @@ __global__ void __launch_bounds__(kMprepThreads) mprep_kernel(
       P.z = elem(i + 2, st, l.z, f.z, make_float2(s23.x, s23.y), ks.z, cn.z);
       P.w = elem(i + 3, st, l.w, f.w, make_float2(s23.z, s23.w), ks.w, cn.w);
       if (write_p) L4[j] = P;
+    };
+    const float4 z4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    for (int j = threadIdx.x; j < n4; j += 2 * bd) {
+      const int j2 = j + bd;
+      const bool two = j2 < n4;
+      const int st = ts ? ts[(size_t)((4 * j) >> 7) * n_rt] : 1;
+      const int st2 = two ? (ts ? ts[(size_t)((4 * j2) >> 7) * n_rt] : 1) : 0;
+      const float4 l = L4[j];
+      const float4 f = st ? F4[j] : z4;
+      const float4 l2 = two ? L4[j2] : z4;
+      const float4 f2 = st2 ? F4[j2] : z4;
+      tuple(j, st, l, f);
+      if (two) tuple(j2, st2, l2, f2);
     }
   } else {
     for (int i = threadIdx.x; i < N; i += blockDim.x) {
@@ -1394,16 +1446,21 @@ extern "C" int emc_plan_bind(emc_plan* p, const float* d_images, const int* d_ma
       if (hmask[q]) pix.push_back(q);
     }
     EMC_REQUIRE(ctx, !pix.empty(), "plan_bind: mask is empty");
-    // Compacted pixels in order of detector radius: the bright low-q pixels,
-    // the only ones whose k^2 needs a second FP16 term, then share a few
-    // k-blocks of the tensor-core E-step (the order is otherwise free: every
-    // compacted array uses it consistently).
+    // Compacted pixels in one-pixel bands of detector radius, each band in
+    // order of angle.  By radius: the bright low-q pixels, the only ones whose
+    // k^2 needs a second FP16 term, share a few k-blocks of the tensor-core
+    // E-step, and the dim outer blocks form the count tail where the G lo
+    // term is dropped.  By angle within a band: the 32 pixels of a warp are
+    // neighbours on the ring, so the expand's model gathers of a warp touch
+    // neighbouring voxels.  (The order is otherwise free: every compacted
+    // array uses it consistently.)
     const int side = p->d.side;
-    auto r2 = [side](int q) {
+    std::vector<std::pair<long long, double>> key(n2);
+    for (int q : pix) {
       const double dx = (double)(q % side) - side / 2 + 0.5, dy = (double)(q / side) - side / 2 + 0.5;
-      return dx * dx + dy * dy;
-    };
-    std::stable_sort(pix.begin(), pix.end(), [&](int a, int b) { return r2(a) < r2(b); });
+      key[q] = {(long long)std::floor(std::sqrt(dx * dx + dy * dy)), std::atan2(dy, dx)};
+    }
+    std::stable_sort(pix.begin(), pix.end(), [&](int a, int b) { return key[a] < key[b]; });
   }
   EMC_REQUIRE(ctx, prev_P == 0 || prev_P == (int)pix.size(),
               "plan_bind: a re-bind must keep the mask's pixel count (%d != %d)", (int)pix.size(),
@@ -1480,11 +1537,13 @@ static int plan_expand(emc_plan* p, const float* model) {
   emc_ctx* ctx = p->ctx;
   const RotOps ops = tc_rot_ops(p);
   if (p->d.interp == EMC_INTERP_NEAREST)
-    slice_rows_kernel<EMC_INTERP_NEAREST><<<p->d.n_rot, 256, 0, ctx->stream>>>(
+    slice_rows_kernel<EMC_INTERP_NEAREST>
+        <<<ceil_div(p->d.n_rot, slice_rows_per_block<EMC_INTERP_NEAREST>()), 256, 0, ctx->stream>>>(
         model, p->d.side, p->rot, p->pix, p->cx, p->cy, p->cz, p->d.n_rot, p->Kp, p->S,
         p->rot_cnt, p->rot_A, p->rot_ssum, ops);
   else
-    slice_rows_kernel<EMC_INTERP_TRILINEAR><<<p->d.n_rot, 256, 0, ctx->stream>>>(
+    slice_rows_kernel<EMC_INTERP_TRILINEAR>
+        <<<ceil_div(p->d.n_rot, slice_rows_per_block<EMC_INTERP_TRILINEAR>()), 256, 0, ctx->stream>>>(
         model, p->d.side, p->rot, p->pix, p->cx, p->cy, p->cz, p->d.n_rot, p->Kp, p->S,
         p->rot_cnt, p->rot_A, p->rot_ssum, ops);
   return after_launch(ctx, "slice_rows_kernel");

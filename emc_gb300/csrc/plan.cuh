@@ -53,9 +53,10 @@ struct emc_plan {
   __half* K2hi = nullptr;    // fp16(k^2 * 2^-e)
   __half* K2lo = nullptr;    // k^2 * 2^-e - K2hi
   unsigned char* k2lo_any = nullptr;  // [Np/128][Kp/32] block has a nonzero K2lo
-  // [Np/128] the likelihood's G lo term runs on the k-blocks below glo_kb[pt]
+  // [Np/128 + 1] the likelihood's G lo term runs on the k-blocks below glo_kb[pt]
   // of pattern tile pt: the blocks after it hold at most glo_tail_ppm / 1e6 of
-  // every pattern's counts (EMC_OPT_GLO_TAIL; 0: G lo on every block)
+  // every pattern's counts (EMC_OPT_GLO_TAIL; 0: G lo on every block);
+  // glo_kb[Np/128] is the largest of them
   int* glo_kb = nullptr;
   int glo_tail_ppm = 1000;
   __half* KhT = nullptr;     // [Kp][Np] transposed counts for the M-step
@@ -204,58 +205,35 @@ struct RotOps {
   __half *Mp = nullptr, *MSh = nullptr, *Gh = nullptr, *Gl = nullptr, *Hh = nullptr, *Hl = nullptr;
   int* flags = nullptr;
   int logs = 0;
+  // device int: G lo is read (and written) only in the 32-pixel blocks below
+  // it, the largest count-tail bound of the pattern tiles (null: every block)
+  const int* gl_end = nullptr;
 };
 
-__device__ __forceinline__ void rot_ops_store(const RotOps& o, size_t e, float s) {
+// The operands of four neighbouring pixels e .. e + 3 (e a multiple of 4) as
+// 8-byte stores; hv = 1 / (s + 0.02) where s > 0 (0 elsewhere), computed by
+// the caller.  The same values as rot_ops_store2, pixel by pixel.
+__device__ __forceinline__ void rot_ops_store4(const RotOps& o, size_t e, const float (&sv)[4],
+                                               const float (&hv)[4], bool g_lo) {
+  union H4 {
+    __half h[4];
+    uint2 u;
+  };
   if (o.logs) {
-    const float l = logf(fmaxf(s, 1e-6f));
-    const __half hi = __float2half_rn(l);
-    o.Gh[e] = hi;
-    o.Gl[e] = __float2half_rn(l - __half2float(hi));
-    return;
-  }
-  // (double)s > 1e-10 of the reference, as a float test: 1e-10f is the first
-  // float above 1e-10, so both agree for every float s
-  const bool mp = s >= 1e-10f;
-  const bool m = s > 0.0f;
-  const float ms = mp ? s * (1.0f / 256.0f) : 0.0f;
-  if (ms > 60000.0f) atomicOr(o.flags, 4);
-  const float h = m ? 1.0f / (s + 0.02f) : 0.0f;
-  const float g = m ? s * h : 0.0f;
-  const __half gh = __float2half_rn(g), hh = __float2half_rn(h);
-  o.Mp[e] = __float2half_rn(mp ? 1.0f : 0.0f);
-  o.MSh[e] = __float2half_rn(ms);
-  o.Gh[e] = gh;
-  if (o.Gl) o.Gl[e] = __float2half_rn(g - __half2float(gh));
-  o.Hh[e] = hh;
-  if (o.Hl) o.Hl[e] = __float2half_rn(h - __half2float(hh));
-}
-
-// The operands of two neighbouring pixels e, e + 1 (e even) as 4-byte stores;
-// h0, h1 = 1 / (s + 0.02) where s > 0 (0 elsewhere), computed by the caller.
-__device__ __forceinline__ void rot_ops_store2(const RotOps& o, size_t e, float s0, float s1,
-                                               float h0, float h1) {
-  const float sv[2] = {s0, s1}, hv[2] = {h0, h1};
-  if (o.logs) {
-    __half2 hi, lo;
-    __half* ph = reinterpret_cast<__half*>(&hi);
-    __half* pl = reinterpret_cast<__half*>(&lo);
+    H4 hi, lo;
 #pragma unroll
-    for (int u = 0; u < 2; ++u) {
+    for (int u = 0; u < 4; ++u) {
       const float l = logf(fmaxf(sv[u], 1e-6f));
-      ph[u] = __float2half_rn(l);
-      pl[u] = __float2half_rn(l - __half2float(ph[u]));
+      hi.h[u] = __float2half_rn(l);
+      lo.h[u] = __float2half_rn(l - __half2float(hi.h[u]));
     }
-    *reinterpret_cast<__half2*>(o.Gh + e) = hi;
-    *reinterpret_cast<__half2*>(o.Gl + e) = lo;
+    *reinterpret_cast<uint2*>(o.Gh + e) = hi.u;
+    *reinterpret_cast<uint2*>(o.Gl + e) = lo.u;
     return;
   }
-  __half2 mp2, ms2, gh2, gl2, hh2, hl2;
-  __half *pmp = reinterpret_cast<__half*>(&mp2), *pms = reinterpret_cast<__half*>(&ms2),
-         *pgh = reinterpret_cast<__half*>(&gh2), *pgl = reinterpret_cast<__half*>(&gl2),
-         *phh = reinterpret_cast<__half*>(&hh2), *phl = reinterpret_cast<__half*>(&hl2);
+  H4 mp4, ms4, gh4, gl4, hh4, hl4;
 #pragma unroll
-  for (int u = 0; u < 2; ++u) {
+  for (int u = 0; u < 4; ++u) {
     const float s = sv[u];
     const bool mp = s >= 1e-10f;
     const bool m = s > 0.0f;
@@ -263,19 +241,19 @@ __device__ __forceinline__ void rot_ops_store2(const RotOps& o, size_t e, float 
     if (ms > 60000.0f) atomicOr(o.flags, 4);
     const float h = hv[u];
     const float g = m ? s * h : 0.0f;
-    pmp[u] = __float2half_rn(mp ? 1.0f : 0.0f);
-    pms[u] = __float2half_rn(ms);
-    pgh[u] = __float2half_rn(g);
-    pgl[u] = __float2half_rn(g - __half2float(pgh[u]));
-    phh[u] = __float2half_rn(h);
-    phl[u] = __float2half_rn(h - __half2float(phh[u]));
+    mp4.h[u] = __float2half_rn(mp ? 1.0f : 0.0f);
+    ms4.h[u] = __float2half_rn(ms);
+    gh4.h[u] = __float2half_rn(g);
+    gl4.h[u] = __float2half_rn(g - __half2float(gh4.h[u]));
+    hh4.h[u] = __float2half_rn(h);
+    hl4.h[u] = __float2half_rn(h - __half2float(hh4.h[u]));
   }
-  *reinterpret_cast<__half2*>(o.Mp + e) = mp2;
-  *reinterpret_cast<__half2*>(o.MSh + e) = ms2;
-  *reinterpret_cast<__half2*>(o.Gh + e) = gh2;
-  if (o.Gl) *reinterpret_cast<__half2*>(o.Gl + e) = gl2;
-  *reinterpret_cast<__half2*>(o.Hh + e) = hh2;
-  if (o.Hl) *reinterpret_cast<__half2*>(o.Hl + e) = hl2;
+  *reinterpret_cast<uint2*>(o.Mp + e) = mp4.u;
+  *reinterpret_cast<uint2*>(o.MSh + e) = ms4.u;
+  *reinterpret_cast<uint2*>(o.Gh + e) = gh4.u;
+  if (o.Gl && g_lo) *reinterpret_cast<uint2*>(o.Gl + e) = gl4.u;
+  *reinterpret_cast<uint2*>(o.Hh + e) = hh4.u;
+  if (o.Hl) *reinterpret_cast<uint2*>(o.Hl + e) = hl4.u;
 }
 
 RotOps tc_rot_ops(emc_plan* p);  // the plan's operand buffers (all null for FP32 plans)

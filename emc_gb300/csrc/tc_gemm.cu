@@ -148,7 +148,8 @@ __device__ __forceinline__ float count_block_sum(const __half* k) {
 
 // One warp per pattern row n: the last 32-pixel block b whose suffix (blocks
 // b ..) still holds more than eps of the row's counts; glo_kb[n / 128] (zeroed
-// before) becomes the largest b + 1 over the tile's rows.  Lane l takes a
+// before) becomes the largest b + 1 over the tile's rows, and glo_kb[n_pt]
+// the largest over all tiles (the expand writes G lo below it).  Lane l takes a
 // contiguous run of blocks: run sums, a warp prefix scan, then a second walk
 // over its run.  Integer counts below 2^24 in total sum exactly in FP32.
 __global__ void __launch_bounds__(256) tc_glo_extent_kernel(const __half* __restrict__ Kh, int Kp,
@@ -177,7 +178,10 @@ __global__ void __launch_bounds__(256) tc_glo_extent_kernel(const __half* __rest
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) last = max(last, __shfl_xor_sync(0xffffffffu, last, o));
-  if (lane == 0 && last >= 0) atomicMax(glo_kb + n / 128, last + 1);
+  if (lane == 0 && last >= 0) {
+    atomicMax(glo_kb + n / 128, last + 1);
+    atomicMax(glo_kb + (N + 127) / 128, last + 1);
+  }
 }
 
 // [rows][cols] -> [cols][rows], FP16: 64 x 64 tiles, moved with 4-byte
@@ -1371,7 +1375,7 @@ int tc_bind(emc_plan* p) {
       if (!rc) rc = plan_alloc(p, (void**)&p->K2hi, pk * 2);
       if (!rc) rc = plan_alloc(p, (void**)&p->K2lo, pk * 2);
       if (!rc) rc = plan_alloc(p, (void**)&p->k2lo_any, (size_t)(Np / 128) * (Kp / 32));
-      if (!rc) rc = plan_alloc(p, (void**)&p->glo_kb, sizeof(int) * (size_t)(Np / 128));
+      if (!rc) rc = plan_alloc(p, (void**)&p->glo_kb, sizeof(int) * (size_t)(Np / 128 + 1));
     }
     __half** rot_ops[6] = {&st->Gh, &st->Gl, &st->Mp, &st->MSh, &st->Hh, &st->Hl};
     for (int j = 0; j < (pois ? 2 : 6); ++j) {
@@ -1449,7 +1453,7 @@ int tc_glo_extent(emc_plan* p) {
   if (!p->glo_kb) return EMC_OK;  // true Poisson: no G operand
   emc_ctx* ctx = p->ctx;
   const int nkb = p->Kp / es::BK, n_pt = p->Np / es::BM;
-  EMC_CUDA(ctx, cudaMemsetAsync(p->glo_kb, 0, sizeof(int) * (size_t)n_pt, ctx->stream));
+  EMC_CUDA(ctx, cudaMemsetAsync(p->glo_kb, 0, sizeof(int) * (size_t)(n_pt + 1), ctx->stream));
   tc_glo_extent_kernel<<<ceil_div(p->d.n_images, 8), 256, 0, ctx->stream>>>(
       p->Kh, p->Kp, nkb, p->d.n_images, (float)p->glo_tail_ppm * 1e-6f, p->glo_kb);
   return after_launch(ctx, "tc_glo_extent_kernel");
@@ -1575,7 +1579,7 @@ static int estep_launch(emc_plan* p, int raster, int first, int count, bool full
   return after_launch(ctx, "tc_estep_kernel");
 }
 
-// The rotation operands were written by the expand (rot_ops_store).
+// The rotation operands are written by the expand (rot_ops_store4).
 int tc_estep(emc_plan* p) { return estep_launch(p, p->estep_raster, 0, INT_MAX, false); }
 
 RotOps tc_rot_ops(emc_plan* p) {
@@ -1596,6 +1600,7 @@ RotOps tc_rot_ops(emc_plan* p) {
     o.Hh = st->Hh;
     o.Gl = (gh & 1) ? st->Gl : nullptr;
     o.Hl = (gh & 2) ? st->Hl : nullptr;
+    if (o.Gl && p->glo_kb) o.gl_end = p->glo_kb + p->Np / es::BM;
   }
   return o;
 }

@@ -858,11 +858,8 @@ namespace ms {
 constexpr int BM = 128;   // rotations per tile (TMEM lanes)
 constexpr int BN = 256;   // pixels per tile
 constexpr int BK = 64;    // patterns per stage (128 B rows, 128B swizzle)
-constexpr int STAGES = 3;
 constexpr int A_BYTES = BM * BK * 2;  // 16 KB
 constexpr int B_BYTES = BN * BK * 2;  // 32 KB
-constexpr int STAGE_BYTES = 2 * A_BYTES + B_BYTES;
-constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 256 + 1024;
 constexpr int EPI_WARPS = 8;          // two per TMEM lane quarter, 128 columns each
 constexpr int THREADS = 64 + 32 * EPI_WARPS;
 }  // namespace ms
@@ -982,22 +979,36 @@ __device__ __forceinline__ void ms_tile(const TcMstepArgs& a, int t, int& r0, in
 // across tiles, and the accumulator is double-buffered in TMEM (columns
 // 0-255 and 256-511), so the insertion epilogue of one tile overlaps the
 // MMAs of the next.
+// Stage ring of the single-CTA M-step: Q hi (+ Q lo) and the 256 K^T rows of
+// a 64-pattern k-block.  Without the Q lo slot a stage is 48 KB and four fit
+// where three of 64 KB do: a third more bytes in flight for the same ring.
+template <int QLO>
+struct MsRing {
+  static constexpr int kStageBytes = (QLO ? 2 : 1) * ms::A_BYTES + ms::B_BYTES;
+  static constexpr int kStages = QLO ? 3 : 4;
+  static constexpr int kOffK = (QLO ? 2 : 1) * ms::A_BYTES;  // K^T tile in a stage
+  static constexpr int kSmem = kStages * kStageBytes + 256 + 1024;
+  static_assert(kSmem <= 232448, "shared memory of the M-step ring");
+};
+
+template <int QLO>
 __global__ void __launch_bounds__(ms::THREADS, 1)
     tc_mstep_kernel(const __grid_constant__ CUtensorMap mQh, const __grid_constant__ CUtensorMap mQl,
                     const __grid_constant__ CUtensorMap mKt, TcMstepArgs a) {
   using namespace ms;
+  using Ring = MsRing<QLO>;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-  uint64_t* full = (uint64_t*)(smem + STAGES * STAGE_BYTES);
-  uint64_t* empty = full + STAGES;
-  uint64_t* tfull = empty + STAGES;  // [2] accumulator ready
+  uint64_t* full = (uint64_t*)(smem + Ring::kStages * Ring::kStageBytes);
+  uint64_t* empty = full + Ring::kStages;
+  uint64_t* tfull = empty + Ring::kStages;  // [2] accumulator ready
   uint64_t* tempty = tfull + 2;      // [2] accumulator drained (one arrival per epilogue warp)
   uint64_t* drain = tempty + 2;      // the MMA issuer's own completion wait before TMEM is freed
   uint32_t* tmem_slot = (uint32_t*)(drain + 1);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (threadIdx.x == 0) {
-    for (int s = 0; s < STAGES; ++s) {
+    for (int s = 0; s < Ring::kStages; ++s) {
       ptx::mbar_init(&full[s], 1);
       ptx::mbar_init(&empty[s], 1);
     }
@@ -1028,20 +1039,20 @@ __global__ void __launch_bounds__(ms::THREADS, 1)
         const int nk = ms_nkb(a, r0 / BM);
         for (int j = 0; j < nk; ++j, ++it) {
           const int kb = ms_kb(a, r0 / BM, j);
-          const int s = it % STAGES;
-          const uint32_t ph = (it / STAGES) & 1;
+          const int s = it % Ring::kStages;
+          const uint32_t ph = (it / Ring::kStages) & 1;
           if (!ptx::mbar_wait(&empty[s], ph ^ 1, a.status, 4, a.spin)) {
             ok = false;
             break;
           }
-          ptx::mbar_arrive_expect_tx(&full[s], STAGE_BYTES - (a.q_lo ? 0 : A_BYTES));
-          unsigned char* st = smem + s * STAGE_BYTES;
+          ptx::mbar_arrive_expect_tx(&full[s], Ring::kStageBytes);
+          unsigned char* st = smem + s * Ring::kStageBytes;
           ptx::tma_load_2d(st, &mQh, kb * BK, r0, &full[s]);
-          if (a.q_lo) ptx::tma_load_2d(st + A_BYTES, &mQl, kb * BK, r0, &full[s]);
-          ptx::tma_load_2d(st + 2 * A_BYTES, &mKt, kb * BK, q0, &full[s]);
+          if (QLO) ptx::tma_load_2d(st + A_BYTES, &mQl, kb * BK, r0, &full[s]);
+          ptx::tma_load_2d(st + Ring::kOffK, &mKt, kb * BK, q0, &full[s]);
         }
       }
-      ptx::drain_loads(full, STAGES, it, a.status, 11);  // none in flight at exit
+      ptx::drain_loads(full, Ring::kStages, it, a.status, 11);  // none in flight at exit
     }
   } else if (warp == 1) {
     // ------------------------------------------------ MMA issuer
@@ -1061,21 +1072,21 @@ __global__ void __launch_bounds__(ms::THREADS, 1)
         // have no responsibility (T_r = 0), so the epilogue inserts nothing
         const int nk = ms_nkb(a, r0t / BM);
         for (int kb = 0; kb < nk; ++kb, ++it) {
-          const int s = it % STAGES;
-          const uint32_t ph = (it / STAGES) & 1;
+          const int s = it % Ring::kStages;
+          const uint32_t ph = (it / Ring::kStages) & 1;
           if (!ptx::mbar_wait(&full[s], ph, a.status, 5, a.spin)) {
             ok = false;
             break;
           }
           ptx::tc_fence_after();
-          const uint32_t base = ptx::smem_u32(smem + s * STAGE_BYTES);
+          const uint32_t base = ptx::smem_u32(smem + s * Ring::kStageBytes);
 #pragma unroll
           for (int ks = 0; ks < BK / 16; ++ks) {
             const uint64_t dQh = ptx::smem_desc(base + ks * 32, 1024, 2);
             const uint64_t dQl = ptx::smem_desc(base + A_BYTES + ks * 32, 1024, 2);
-            const uint64_t dK = ptx::smem_desc(base + 2 * A_BYTES + ks * 32, 1024, 2);
+            const uint64_t dK = ptx::smem_desc(base + Ring::kOffK + ks * 32, 1024, 2);
             ptx::mma_f16(d, dQh, dK, idesc, (kb | ks) ? 1u : 0u);
-            if (a.q_lo) ptx::mma_f16(d, dQl, dK, idesc, 1u);
+            if (QLO) ptx::mma_f16(d, dQl, dK, idesc, 1u);
           }
           ptx::mma_commit(&empty[s]);
         }
@@ -1412,8 +1423,12 @@ int tc_bind(emc_plan* p) {
                                        es2::SMEM_BYTES));
     EMC_CUDA(ctx, cudaFuncSetAttribute(tc_estep_pois_kernel,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, ep::SMEM_BYTES));
-    EMC_CUDA(ctx, cudaFuncSetAttribute(tc_mstep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       ms::SMEM_BYTES));
+    EMC_CUDA(ctx, cudaFuncSetAttribute(tc_mstep_kernel<0>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       MsRing<0>::kSmem));
+    EMC_CUDA(ctx, cudaFuncSetAttribute(tc_mstep_kernel<1>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       MsRing<1>::kSmem));
     EMC_CUDA(ctx, cudaFuncSetAttribute(tc_mstep_pair_kernel,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        ms2::SMEM_BYTES));
@@ -1763,7 +1778,12 @@ int tc_mstep(emc_plan* p, float* model, float* weight) {
     p->mstep_pair = 0;
   }
   const int grid = std::min(a.n_tiles, ctx->sm_count);
-  tc_mstep_kernel<<<grid, ms::THREADS, ms::SMEM_BYTES, ctx->stream>>>(st->mQh, st->mQl, st->mKt, a);
+  if (a.q_lo)
+    tc_mstep_kernel<1><<<grid, ms::THREADS, MsRing<1>::kSmem, ctx->stream>>>(st->mQh, st->mQl,
+                                                                              st->mKt, a);
+  else
+    tc_mstep_kernel<0><<<grid, ms::THREADS, MsRing<0>::kSmem, ctx->stream>>>(st->mQh, st->mQl,
+                                                                              st->mKt, a);
   return after_launch(ctx, "tc_mstep_kernel");
 }
 

@@ -1756,13 +1756,17 @@ static int iterate_enqueue(emc_plan* p, float* d_model, float* d_weight) {
   return enqueue_finish(p, d_model, d_weight);
 }
 
+// Writes one float on a stream with a kernel rather than a host-to-device
+// copy: a copy would queue on the copy engine behind any bulk host copy that
+// another stream has issued (the next patterns, uploaded while this iteration
+// runs) and hold the iteration back until that copy ends.
+__global__ void set_float_kernel(float* __restrict__ dst, float v) { *dst = v; }
+
 static int set_sigma(emc_plan* p, float sigma) {
   emc_ctx* ctx = p->ctx;
   EMC_REQUIRE(ctx, sigma > 0.0f && std::isfinite(sigma), "iterate: bad sigma");
-  // pageable source: staged before the call returns, ordered on the stream
-  EMC_CUDA(ctx, cudaMemcpyAsync(p->sigma_dev, &sigma, sizeof(float), cudaMemcpyHostToDevice,
-                                ctx->stream));
-  return EMC_OK;
+  set_float_kernel<<<1, 1, 0, ctx->stream>>>(p->sigma_dev, sigma);
+  return after_launch(ctx, "set_float_kernel");
 }
 
 extern "C" int emc_iterate_async(emc_plan* p, float* d_model, float* d_weight, float sigma) {
@@ -1919,9 +1923,9 @@ extern "C" int emc_batch_run(emc_batch* b, const float* sigmas) {
   for (size_t k = 0; k < b->plans.size(); ++k) {
     const float sg = sigmas[k];
     EMC_REQUIRE(ctx, sg > 0.0f && std::isfinite(sg), "batch_run: bad sigma %zu", k);
-    // pageable source: staged before the call returns, ordered before the launch
-    EMC_CUDA(ctx, cudaMemcpyAsync(b->plans[k]->sigma_dev, &sg, sizeof(float),
-                                  cudaMemcpyHostToDevice, ctx->stream));
+    set_float_kernel<<<1, 1, 0, ctx->stream>>>(b->plans[k]->sigma_dev, sg);
+    int rc = after_launch(ctx, "set_float_kernel");
+    if (rc) return rc;
   }
   EMC_CUDA(ctx, cudaGraphLaunch(b->exec, ctx->stream));
   return EMC_OK;

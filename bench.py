@@ -69,8 +69,11 @@ def parse():
                          "the large configuration, 10 for mid, 0 otherwise)")
     ap.add_argument("--estep-pair", type=int, choices=[0, 1], default=1,
                     help="tensor path: full likelihood scans on CTA pairs (EMC_OPT_ESTEP_PAIR)")
-    ap.add_argument("--mstep-pair", type=int, choices=[0, 1], default=0,
+    ap.add_argument("--mstep-pair", type=int, choices=[0, 1], default=1,
                     help="tensor path: full-scan M-step on CTA pairs (EMC_OPT_MSTEP_PAIR)")
+    ap.add_argument("--mstep-raster", type=int, default=0,
+                    help="tensor path: the M-step's tile order (EMC_OPT_MSTEP_RASTER); 0: the "
+                         "library's default")
     ap.add_argument("--raster", type=int, default=0,
                     help="tensor path: the likelihood kernel's tile order (EMC_OPT_ESTEP_RASTER); "
                          "0 (default): chosen by emc_plan_autotune before the warm-up")
@@ -311,6 +314,8 @@ def run_ours(args):
             p.set_option(E.Plan.OPT_COUNTS_ROUND, 1)
         p.set_option(E.Plan.OPT_ESTEP_PAIR, args.estep_pair)
         p.set_option(E.Plan.OPT_MSTEP_PAIR, args.mstep_pair)
+        if args.mstep_raster:
+            p.set_option(E.Plan.OPT_MSTEP_RASTER, args.mstep_raster)
         p.bind(images, mask, x, y, z, rot, w)
         return p
 

@@ -116,7 +116,7 @@ struct emc_plan {
   int mstep_raster = -16;   // tensor M-step tile order (EMC_OPT_MSTEP_RASTER)
   int mstep_aggregate = 0;  // tensor M-step: warp-aggregated float atomics (nearest)
   unsigned debug_spin = 0;  // > 0: polls per tensor-pipeline wait (EMC_OPT_DEBUG_SPIN)
-  int mstep_pair = 0;       // tensor M-step full scans on CTA pairs (EMC_OPT_MSTEP_PAIR)
+  int mstep_pair = 1;       // tensor M-step full scans on CTA pairs (EMC_OPT_MSTEP_PAIR)
 
   // sorted-voxel insertion (EMC_INSERT_SORTED, sorted_insert.cu): the M-step
   // stores each pair's value T_r x slice in ins_u [P_eff][ins_ldu] (rotation

@@ -1164,21 +1164,29 @@ __global__ void __launch_bounds__(ms::THREADS, 1)
 // `tfull`; the epilogue warps of both CTAs hand a buffer back on rank 0's
 // `tempty`.  Full scans only (a pruned M-step runs single CTAs).
 namespace ms2 {
-constexpr int STAGES = 4;
-constexpr int A_BYTES = ms::BM * ms::BK * 2;        // 16 KB: 128 rotations x 64 patterns
-constexpr int B_BYTES = 128 * ms::BK * 2;           // 16 KB: 128 pixels x 64 patterns
-constexpr int STAGE_BYTES = 2 * A_BYTES + B_BYTES;  // Q hi, Q lo, K^T half
-constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 256 + 1024;
-static_assert(SMEM_BYTES <= 232448, "shared memory of the pair M-step");
+constexpr int A_BYTES = ms::BM * ms::BK * 2;  // 16 KB: 128 rotations x 64 patterns
+constexpr int B_BYTES = 128 * ms::BK * 2;     // 16 KB: 128 pixels x 64 patterns
+// stage: Q hi (+ Q lo) and the CTA's half of K^T; six 32 KB stages without
+// the Q lo slot, four of 48 KB with it
+template <int QLO>
+struct Ring {
+  static constexpr int kStageBytes = (QLO ? 2 : 1) * A_BYTES + B_BYTES;
+  static constexpr int kStages = QLO ? 4 : 6;
+  static constexpr int kOffK = (QLO ? 2 : 1) * A_BYTES;
+  static constexpr int kSmem = kStages * kStageBytes + 256 + 1024;
+  static_assert(kSmem <= 232448, "shared memory of the pair M-step");
+};
 }  // namespace ms2
 
+template <int QLO>
 __global__ void __launch_bounds__(ms::THREADS, 1)
     tc_mstep_pair_kernel(const __grid_constant__ CUtensorMap mQh,
                          const __grid_constant__ CUtensorMap mQl,
                          const __grid_constant__ CUtensorMap mKt128, TcMstepArgs a) {
   using namespace ms;
-  using ms2::STAGES;
-  using ms2::STAGE_BYTES;
+  constexpr int STAGES = ms2::Ring<QLO>::kStages;
+  constexpr int STAGE_BYTES = ms2::Ring<QLO>::kStageBytes;
+  constexpr int OFF_K = ms2::Ring<QLO>::kOffK;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   uint64_t* full = (uint64_t*)(smem + STAGES * STAGE_BYTES);
@@ -1220,7 +1228,7 @@ __global__ void __launch_bounds__(ms::THREADS, 1)
     if (lane == 0) {
       uint32_t it = 0;
       bool ok = true;
-      const uint32_t bytes = (a.q_lo ? 2 : 1) * ms2::A_BYTES + ms2::B_BYTES;
+      const uint32_t bytes = STAGE_BYTES;
       for (int t = cl; t < n_tiles && ok; t += ncl) {
         int qt, rp;
         raster_tile(t, a.raster, a.n_qt, n_rp, qt, rp);
@@ -1236,8 +1244,8 @@ __global__ void __launch_bounds__(ms::THREADS, 1)
           const uint32_t fb = ptx::mapa_shared(ptx::smem_u32(&full[s]), 0);
           unsigned char* st = smem + s * STAGE_BYTES;
           ptx::tma_load_2d_pair(st, &mQh, kb * BK, r0, fb);
-          if (a.q_lo) ptx::tma_load_2d_pair(st + ms2::A_BYTES, &mQl, kb * BK, r0, fb);
-          ptx::tma_load_2d_pair(st + 2 * ms2::A_BYTES, &mKt128, kb * BK, q0, fb);
+          if (QLO) ptx::tma_load_2d_pair(st + ms2::A_BYTES, &mQl, kb * BK, r0, fb);
+          ptx::tma_load_2d_pair(st + OFF_K, &mKt128, kb * BK, q0, fb);
         }
       }
       // rank 0's barriers count both CTAs' bytes of the stages it armed
@@ -1268,9 +1276,9 @@ __global__ void __launch_bounds__(ms::THREADS, 1)
           for (int ks = 0; ks < BK / 16; ++ks) {
             const uint64_t dQh = ptx::smem_desc(base + ks * 32, 1024, 2);
             const uint64_t dQl = ptx::smem_desc(base + ms2::A_BYTES + ks * 32, 1024, 2);
-            const uint64_t dK = ptx::smem_desc(base + 2 * ms2::A_BYTES + ks * 32, 1024, 2);
+            const uint64_t dK = ptx::smem_desc(base + OFF_K + ks * 32, 1024, 2);
             ptx::mma_f16_pair(d, dQh, dK, idesc, (kb | ks) ? 1u : 0u);
-            if (a.q_lo) ptx::mma_f16_pair(d, dQl, dK, idesc, 1u);
+            if (QLO) ptx::mma_f16_pair(d, dQl, dK, idesc, 1u);
           }
           ptx::mma_commit_pair(&empty[s], 0x3);
         }
@@ -1429,9 +1437,12 @@ int tc_bind(emc_plan* p) {
     EMC_CUDA(ctx, cudaFuncSetAttribute(tc_mstep_kernel<1>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        MsRing<1>::kSmem));
-    EMC_CUDA(ctx, cudaFuncSetAttribute(tc_mstep_pair_kernel,
+    EMC_CUDA(ctx, cudaFuncSetAttribute(tc_mstep_pair_kernel<0>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       ms2::SMEM_BYTES));
+                                       ms2::Ring<0>::kSmem));
+    EMC_CUDA(ctx, cudaFuncSetAttribute(tc_mstep_pair_kernel<1>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       ms2::Ring<1>::kSmem));
   }
   if (p->mstep_q_lo && (rc = tc_ensure_qlo(p))) return rc;
   // counts already in FP16 from the bind's pattern pass when its scale holds
@@ -1761,7 +1772,7 @@ int tc_mstep(emc_plan* p, float* model, float* weight) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(2 * clusters);
     cfg.blockDim = dim3(ms::THREADS);
-    cfg.dynamicSmemBytes = ms2::SMEM_BYTES;
+    cfg.dynamicSmemBytes = a.q_lo ? ms2::Ring<1>::kSmem : ms2::Ring<0>::kSmem;
     cfg.stream = ctx->stream;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
@@ -1771,7 +1782,8 @@ int tc_mstep(emc_plan* p, float* model, float* weight) {
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     const cudaError_t e =
-        cudaLaunchKernelEx(&cfg, tc_mstep_pair_kernel, st->mQh, st->mQl, st->mKt128, a);
+        a.q_lo ? cudaLaunchKernelEx(&cfg, tc_mstep_pair_kernel<1>, st->mQh, st->mQl, st->mKt128, a)
+               : cudaLaunchKernelEx(&cfg, tc_mstep_pair_kernel<0>, st->mQh, st->mQl, st->mKt128, a);
     if (e == cudaSuccess) return after_launch(ctx, "tc_mstep_pair_kernel");
     // a refused launch configuration is not a sticky error: single CTAs from now on
     (void)cudaGetLastError();

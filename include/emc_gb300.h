@@ -486,10 +486,11 @@ int emc_batch_destroy(emc_batch* batch);
  * frees its TMEM and exits, so no copy or MMA is in flight when a CTA leaves.
  * The next iteration with the default is unaffected. */
 #define EMC_OPT_DEBUG_SPIN 9
-/* EMC_OPT_MSTEP_PAIR: 1 runs the full-scan tensor-core M-step on clusters of
- * two CTAs (256 rotations x 256 pixels per pair, 256-row MMAs), 0 (default)
- * on single CTAs (128 x 256); at 128^3 the pairs measured 9.9 ms against
- * 9.5 ms.  Pruned iterations always use single CTAs;
+/* EMC_OPT_MSTEP_PAIR: 1 (default) runs the full-scan tensor-core M-step on
+ * clusters of two CTAs (256 rotations x 256 pixels per pair, 256-row MMAs,
+ * half of the pixel-side operand per CTA), 0 on single CTAs (128 x 256); at
+ * 128^3 the pairs measured 6.7 ms against 8.4 ms.  Pruned iterations always
+ * use single CTAs;
  * where a cluster launch is refused the plan falls back to single CTAs.
  * Results do not depend on it (bit for bit with deterministic insertion). */
 #define EMC_OPT_MSTEP_PAIR 10

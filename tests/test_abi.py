@@ -74,6 +74,12 @@ def test_option_numbers_match_the_header(built):
     assert len(opts) >= 7
     for name, value in opts.items():
         assert getattr(E.Plan, "OPT_" + name) == value, name
+    # insertion modes likewise (EMC_INSERT_* -> emc_gb300.INSERT_*)
+    modes = {m.group(1): int(m.group(2))
+             for m in re.finditer(r"#define EMC_INSERT_([A-Z0-9_]+) (-?\d+)", hdr)}
+    assert set(modes) == {"ATOMIC", "DETERMINISTIC", "SORTED"}
+    for name, value in modes.items():
+        assert getattr(E, "INSERT_" + name) == value, name
 
 
 def test_heldout_patterns_share_the_particle():

@@ -345,7 +345,10 @@ def run_ours(args):
             t0 = time.perf_counter()
             r, ms = plan.autotune(model, sig[0])
             tuning = {"estep_raster": r, "source": "emc_plan_autotune",
+                      "estep_pair": plan.get_option(E.Plan.OPT_ESTEP_PAIR),
                       "prefix_ms": ms, "tuning_s": time.perf_counter() - t0}
+        # the autotuner may have chosen single-CTA likelihood tiles
+        args.estep_pair = plan.get_option(E.Plan.OPT_ESTEP_PAIR)
     for i in range(args.warmup):
         plan.iterate(model, weight, sig[i], stats=False)
     torch.cuda.synchronize()

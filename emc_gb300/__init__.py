@@ -462,6 +462,12 @@ class Plan:
     def set_option(self, option: int, value: int):
         self.ctx._check(self._lib.emc_plan_set_option(self._h, option, value), "plan_set_option")
 
+    def get_option(self, option: int) -> int:
+        v = C.c_int(0)
+        self.ctx._check(self._lib.emc_plan_get_option(self._h, option, C.byref(v)),
+                        "plan_get_option")
+        return v.value
+
     def autotune(self, model, sigma: float = 0.4) -> tuple:
         """Picks the likelihood kernel's tile order (OPT_ESTEP_RASTER) by
         timing the candidates on `model` (emc_plan_autotune).  Returns

@@ -156,6 +156,7 @@ SIGNATURES: dict[str, tuple] = {
     "emc_model_from_sums": (I, [P, P, P, I, P, P]),
     "emc_plan_set_profiling": (I, [P, I]),
     "emc_plan_set_option": (I, [P, I, I]),
+    "emc_plan_get_option": (I, [P, I, P]),
     "emc_plan_autotune": (I, [P, P, F, C.POINTER(I), C.POINTER(F)]),
     "emc_plan_time_likelihood": (I, [P, P, F, I, I, I, C.POINTER(F), C.POINTER(I)]),
     "emc_tc_gemm_selftest": (I, [P, P, P, P, I, I]),

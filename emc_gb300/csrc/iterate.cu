@@ -1955,6 +1955,24 @@ extern "C" int emc_batch_destroy(emc_batch* b) {
   return EMC_OK;
 }
 
+extern "C" int emc_plan_get_option(const emc_plan* p, int option, int* value) {
+  if (!p || !value) return EMC_ERR_INVALID;
+  emc_ctx* ctx = p->ctx;
+  switch (option) {
+    case EMC_OPT_MSTEP_QLO: *value = p->mstep_q_lo; return EMC_OK;
+    case EMC_OPT_ESTEP_GHLO: *value = p->estep_gh_lo; return EMC_OK;
+    case EMC_OPT_MSTEP_AGGREGATE: *value = p->mstep_aggregate; return EMC_OK;
+    case EMC_OPT_COUNTS_ROUND: *value = p->counts_round; return EMC_OK;
+    case EMC_OPT_ESTEP_RASTER: *value = p->estep_raster; return EMC_OK;
+    case EMC_OPT_ESTEP_PAIR: *value = p->estep_pair; return EMC_OK;
+    case EMC_OPT_MSTEP_RASTER: *value = p->mstep_raster; return EMC_OK;
+    case EMC_OPT_DEBUG_SPIN: *value = (int)p->debug_spin; return EMC_OK;
+    case EMC_OPT_MSTEP_PAIR: *value = p->mstep_pair; return EMC_OK;
+    case EMC_OPT_GLO_TAIL: *value = p->glo_tail_ppm; return EMC_OK;
+    default: return fail(ctx, EMC_ERR_INVALID, "plan_get_option: unknown option %d", option);
+  }
+}
+
 extern "C" int emc_plan_set_option(emc_plan* p, int option, int value) {
   if (!p) return EMC_ERR_INVALID;
   emc_ctx* ctx = p->ctx;

@@ -1722,9 +1722,35 @@ int tc_autotune(emc_plan* p, int waves, int* best, float* best_ms) {
   for (size_t j = 1; j < cand.size(); ++j)
     if (t[j] < t[b]) b = j;
   if (t[0] <= 1.02f * t[b]) b = 0;
-  p->estep_raster = cand[b];
-  if (best) *best = cand[b];
-  if (best_ms) *best_ms = t[b];
+  int raster = cand[b];
+  float raster_ms = t[b];
+  // tile shape: CTA pairs (256 patterns x 128 rotations, 256-row MMAs) or
+  // single CTAs (128 x 128).  The single-CTA kernel, in its default order,
+  // is timed on the same windows in its own tile units (twice the tiles,
+  // the same (pattern, rotation) work); it replaces the pairs when 2 %
+  // faster.  The shapes' results differ only by the FP32 rounding of the
+  // accumulation (1e-6 relative).
+  if (pair) {
+    p->estep_pair = 0;
+    const int s_total = (p->Np / 128) * n_rt;
+    const int s_count = std::min(s_total, 2 * count);
+    float ts = 0.0f;
+    for (int first : firsts) {
+      float ms = 0.0f;
+      if ((rc = tc_time_estep(p, 8, std::min(2 * first, s_total - s_count), s_count, &ms))) break;
+      ts = std::max(ts, ms);
+    }
+    if (!rc && ts < 0.98f * raster_ms) {
+      raster = 8;
+      raster_ms = ts;
+    } else {
+      p->estep_pair = 1;
+    }
+    if (rc) return rc;
+  }
+  p->estep_raster = raster;
+  if (best) *best = raster;
+  if (best_ms) *best_ms = raster_ms;
   return EMC_OK;
 }
 

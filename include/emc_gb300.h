@@ -503,12 +503,18 @@ int emc_batch_destroy(emc_batch* batch);
  * once when the plan is bound. */
 #define EMC_OPT_GLO_TAIL 11
 int emc_plan_set_option(emc_plan* plan, int option, int value);
-/* Tile-order autotuner of the tensor-core likelihood kernel: expands d_model
- * (sigma as in emc_iterate), times the kernel for each candidate
- * EMC_OPT_ESTEP_RASTER order on two windows of 256 waves of the SMs inside
- * its tile grid (the whole grid when smaller), scores each order by its
- * slower window and sets the fastest; *h_raster / *h_ms (may be NULL)
- * receive it and that time.  Synchronous.  Overwrites the plan's responsibilities and scaling
+/* The option's current value (after emc_plan_autotune: the tile order and
+ * shape it chose). */
+int emc_plan_get_option(const emc_plan* plan, int option, int* value);
+/* Tile-order and tile-shape autotuner of the tensor-core likelihood kernel:
+ * expands d_model (sigma as in emc_iterate), times the kernel for each
+ * candidate EMC_OPT_ESTEP_RASTER order on two windows of 256 waves of the SMs
+ * inside its tile grid (the whole grid when smaller), scores each order by
+ * its slower window and sets the fastest; with CTA pairs in use it then times
+ * single-CTA tiles (128 x 128 instead of 256 x 128 patterns x rotations) on
+ * the same windows and switches EMC_OPT_ESTEP_PAIR off when they are 2 %
+ * faster (the two shapes' results differ by FP32 accumulation rounding,
+ * 1e-6 relative).  *h_raster / *h_ms (may be NULL) receive the order and its time.  Synchronous.  Overwrites the plan's responsibilities and scaling
  * (the next emc_iterate rewrites them); d_model is not changed.  FP32 plans
  * have no tile order: *h_raster = 0.  Results of later iterations do not
  * depend on the order. */

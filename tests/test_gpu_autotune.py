@@ -63,8 +63,12 @@ def test_autotune_picks_a_candidate(ctx, cuda, prob, diff):
     raster, ms = plan.autotune(m, 0.3)
     assert raster != 0 and abs(raster) <= CANDIDATES_MAX and ms > 0.0
     assert torch.equal(m, m0)  # the model is only read
-    # the tuned plan iterates like one with the default order
+    # the tuned plan iterates like one with the default order and the tile
+    # shape the tuner kept (CTA pairs or single CTAs)
     ref, _ = bound(ctx, prob, cuda, precision=E.PREC_MIXED, diff=diff)
+    shape = plan.get_option(E.Plan.OPT_ESTEP_PAIR)
+    assert shape in (0, 1)
+    ref.set_option(E.Plan.OPT_ESTEP_PAIR, shape)
     m1, w1 = m0.clone(), torch.empty_like(m0)
     w = torch.empty_like(m0)
     st = plan.iterate(m, w, 0.3)
@@ -99,4 +103,21 @@ def test_mstep_orders_give_identical_iterations(ctx, cuda, prob):
     for bad in (0, 4097):
         with pytest.raises(E.EmcError):
             plan.set_option(E.Plan.OPT_MSTEP_RASTER, bad)
+    plan.close()
+
+
+def test_option_values_read_back(ctx, cuda, prob):
+    """emc_plan_get_option returns what emc_plan_set_option set (and the
+    defaults before)."""
+    plan, _ = bound(ctx, prob, cuda, precision=E.PREC_MIXED)
+    assert plan.get_option(E.Plan.OPT_ESTEP_PAIR) == 1
+    assert plan.get_option(E.Plan.OPT_MSTEP_PAIR) == 1
+    assert plan.get_option(E.Plan.OPT_GLO_TAIL) == 1000
+    for opt, val in ((E.Plan.OPT_ESTEP_RASTER, -19), (E.Plan.OPT_MSTEP_RASTER, 8),
+                     (E.Plan.OPT_ESTEP_PAIR, 0), (E.Plan.OPT_GLO_TAIL, 0),
+                     (E.Plan.OPT_MSTEP_QLO, 1)):
+        plan.set_option(opt, val)
+        assert plan.get_option(opt) == val
+    with pytest.raises(E.EmcError):
+        plan.get_option(999)
     plan.close()

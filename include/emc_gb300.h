@@ -464,9 +464,10 @@ int emc_batch_destroy(emc_batch* batch);
 #define EMC_OPT_ESTEP_RASTER 6
 /* EMC_OPT_ESTEP_PAIR: 1 (default) runs full scans of the reference
  * likelihood on clusters of two CTAs with 256-row MMAs (each CTA stores half
- * of the rotation-side operands, which cuts the shared-memory traffic that
- * bounds the single-CTA kernel); 0 runs every scan on single CTAs.  Pruned
- * iterations always use single CTAs.  Results are the same either way. */
+ * of the rotation-side operands); 0 runs every scan on single CTAs.
+ * emc_plan_autotune may switch it off where single CTAs are faster.  Pruned
+ * iterations always use single CTAs.  The log-likelihoods agree to FP32
+ * accumulation rounding (1e-6 relative). */
 #define EMC_OPT_ESTEP_PAIR 7
 /* EMC_OPT_MSTEP_RASTER: order of the persistent tensor-core M-step's
  * (rotation tile, pixel tile) work: g > 0 groups of g rotation tiles running
@@ -492,7 +493,8 @@ int emc_batch_destroy(emc_batch* batch);
  * 128^3 the pairs measured 6.7 ms against 8.4 ms.  Pruned iterations always
  * use single CTAs;
  * where a cluster launch is refused the plan falls back to single CTAs.
- * Results do not depend on it (bit for bit with deterministic insertion). */
+ * The two shapes' models agree to FP32 accumulation rounding (1e-5
+ * relative). */
 #define EMC_OPT_MSTEP_PAIR 10
 /* EMC_OPT_GLO_TAIL: the likelihood's G lo term (the FP16 lo half of
  * G = s/(s+c) in B = K.G^T) is applied per 128-pattern tile up to the last

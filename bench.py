@@ -306,7 +306,9 @@ def run_ours(args):
 
     def new_plan(prec):
         diff = E.DIFF_TRUE_POISSON if args.diff == "true_poisson" else E.DIFF_POISSON
-        p = E.Plan(ctx, s, N, R, diff=diff, precision=prec, insert_mode=insert)
+        # the configuration's blur of the new model (the small configuration: sigma 1)
+        p = E.Plan(ctx, s, N, R, diff=diff, precision=prec, insert_mode=insert,
+                   blur_sigma=prob.cfg.blur)
         p.set_option(E.Plan.OPT_MSTEP_QLO, args.mstep_qlo)
         p.set_option(E.Plan.OPT_ESTEP_GHLO, args.estep_ghlo)
         p.set_option(E.Plan.OPT_MSTEP_AGGREGATE, args.mstep_aggregate)

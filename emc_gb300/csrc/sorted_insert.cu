@@ -320,7 +320,8 @@ __global__ void sv_piece_fill_kernel(const uint32_t* __restrict__ seg,
        v += stride) {
     const uint32_t s0 = seg[v], s1 = seg[v + 1];
     uint32_t o = off[v];
-    for (uint32_t s = s0; s < s1; s += kPiece, ++o) piece[o] = make_uint2(s, min(s + kPiece, s1));
+    for (unsigned long long s = s0; s < s1; s += kPiece, ++o)
+      piece[o] = make_uint2((uint32_t)s, (uint32_t)min(s + kPiece, (unsigned long long)s1));
   }
 }
 
@@ -425,7 +426,8 @@ int build(emc_plan* p, SortedInsert* s) {
   const int pb = std::max(1, bits_for((unsigned long long)(P - 1)));
   const int cb = tri ? 3 : 0;
   const long long n = (long long)R * P * C;
-  if (rb + pb + cb > 32 || n >= (1LL << 32))
+  // entry indices stay 32-bit with room for a piece past the last entry
+  if (rb + pb + cb > 32 || n >= (1LL << 32) - 1024)
     return fail(ctx, EMC_ERR_UNSUPPORTED,
                 "sorted insertion: %d rotations x %d pixels%s do not fit 32-bit pair codes", R, P,
                 tri ? " x 8 corners" : "");

@@ -804,7 +804,7 @@ __global__ void finite_sum_kernel(const double* __restrict__ x, int n, double* _
 //   when Ql != nullptr), each row scaled by 2^e_r so its largest entry sits
 //   near 2^14 (qscale_r = 2^-e_r); with stage, the row is kept in shared
 //   memory between the two passes, else the second pass re-reads it.
-constexpr int kMprepThreads = 512;  // two blocks per SM (60 registers per thread)
+constexpr int kMprepThreads = 512;  // two blocks per SM (at most 64 registers per thread)
 constexpr int kMprepStageMax = 30720;  // patterns whose row of Q fits shared memory (120 KB)
 
 __global__ void __launch_bounds__(kMprepThreads, 2) mprep_kernel(

@@ -37,6 +37,11 @@ def test_null_context_is_rejected(built):
     assert lib.emc_get_slices(None, None, 8, None, None, None, None, None, 0, 1, 0) == -1
     assert lib.emc_last_error(None) == b"null context"
     assert lib.emc_plan_bind(None, None, None, None, None, None, None, None) == -1
+    # option access on a null plan (no device work) is refused, not dereferenced
+    import ctypes
+    v = ctypes.c_int(7)
+    assert lib.emc_plan_get_option(None, 3, ctypes.byref(v)) == -1 and v.value == 7
+    assert lib.emc_plan_set_option(None, 3, 1) == -1
 
 
 def test_sigma_schedule_matches_main_cpp(built):
